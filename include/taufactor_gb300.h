@@ -1,0 +1,136 @@
+/*
+ * taufactor_gb300 C ABI: GB300 (sm_103a) kernels for TauFactor's steady-state voxel
+ * diffusion solve (red-black over-relaxed Jacobi on the 7-point stencil).
+ *
+ * The reference (tldr-group/taufactor v1.2.1) is pure Python on torch eager ops and has no FFI;
+ * each entry point below replaces one torch op sequence of its solve path, cited per function
+ * as taufactor/taufactor.py:<lines>.
+ *
+ * Conventions
+ *  - Every pointer argument named *_dev is device memory owned by the caller (the Python host
+ *    uses torch's caching allocator). The library borrows pointers for the call and frees nothing.
+ *  - `stream` is a cudaStream_t passed as void*; NULL means the legacy default stream. All
+ *    launches are asynchronous and stream-ordered; no entry point synchronises the host except
+ *    where stated.
+ *  - Return value: TF_OK or one of the TF_ERR_* codes; tf_status_string() names them.
+ *  - Geometry: volumes of one batch share one shape. Voxel (x, y, z) of volume b lives in the
+ *    "z-parity split" layout: row (b, x, y) holds the even-z half-row, then the odd-z half-row,
+ *    each with `halo_j` ghost cells on both sides; rows have `halo_y` ghost rows on both y sides.
+ *    Ghost cells hold 0 (closed faces) or copies of the wrapped interior (periodic faces).
+ *    tf_geometry() computes the pitches and buffer sizes.
+ */
+#ifndef TAUFACTOR_GB300_H
+#define TAUFACTOR_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TF_OK 0
+#define TF_ERR_ARG 1         /* invalid argument (shape, pointer, alignment, sizes)        */
+#define TF_ERR_CUDA 2        /* a CUDA runtime call failed                                 */
+#define TF_ERR_TIMEOUT 3     /* a bounded device-side wait ran out; kernel returned early   */
+#define TF_ERR_UNSUPPORTED 4 /* valid request this build does not handle                    */
+#define TF_ERR_NOTCONV 5     /* iteration limit reached before convergence                  */
+
+/* operator kinds */
+#define TF_KIND_BINARY 0      /* Solver / PeriodicSolver: divisor = conductive-neighbour count  */
+#define TF_KIND_ANISOTROPIC 1 /* AnisotropicSolver: y, z neighbours weighted by ky, kz          */
+#define TF_KIND_MULTIPHASE 2  /* MultiPhaseSolver(s): harmonic-mean face conductances          */
+
+/* periodic flags */
+#define TF_PERIODIC_Y 1
+#define TF_PERIODIC_Z 2
+
+#define TF_MAX_PHASES 31      /* multiphase: phase indices 1..31; index 0 = outside the volume */
+#define TF_MAX_HALF_SWEEPS 4  /* half-sweeps fused into one tiled launch (= ghost rows)        */
+
+typedef struct tf_geom {
+    int32_t batch, nx, ny, nz; /* interior extents (x = transport axis)                       */
+    int32_t halo_y;            /* ghost rows on each y side                                   */
+    int32_t halo_j;            /* ghost cells on each side of each z-parity half-row           */
+    int32_t yp;                /* rows per x-plane = ny + 2*halo_y                             */
+    int32_t zh;                /* floats per half-row (multiple of 4)                          */
+    int32_t zhc;               /* bytes per half-row of the code buffer (multiple of 16)       */
+    int32_t tiled;             /* 1 if the tiled multi-half-sweep kernel can run this shape    */
+    int64_t field_elems;       /* floats in one field buffer (whole batch)                    */
+    int64_t code_bytes;        /* bytes in one code buffer (whole batch)                      */
+} tf_geom;
+
+typedef struct tf_operator {
+    int32_t kind;              /* TF_KIND_*                                                    */
+    int32_t periodic;          /* TF_PERIODIC_* bits                                           */
+    float omega;               /* float32 over-relaxation factor                               */
+    float ghost_lo, ghost_hi;  /* Dirichlet ghost values 2*bc: -1 (x = -1) and +1 (x = nx)     */
+    float ky, kz;              /* anisotropic y, z weights (dx/dy)^2, (dx/dz)^2                */
+    int32_t n_phases;          /* multiphase: phases 1..n_phases                               */
+    float divisor[256];        /* binary/anisotropic: code -> diagonal (inf = frozen voxel)    */
+    float face[32 * 32];       /* multiphase: [phase a][phase b] harmonic face conductance     */
+    uint8_t conductive[32];    /* multiphase: phase -> D > 0 (mask of the initial field)       */
+} tf_operator;
+
+/* Library version string. */
+const char* tf_version(void);
+
+/* Human-readable name of a TF_* status code. */
+const char* tf_status_string(int status);
+
+/* Number of CUDA kernels this library has launched since load (for launch accounting). */
+int64_t tf_launch_count(void);
+
+/* Fill *out with pitches and buffer sizes for a batch of `batch` volumes of nx*ny*nz voxels.
+ * Pure host arithmetic. `periodic` selects which shapes the tiled kernel accepts. */
+int tf_geometry(int batch, int nx, int ny, int nz, int periodic, tf_geom* out);
+
+/* Build the code buffer and the initial field from per-voxel phase indices.
+ * Replaces ThroughTransportSolver.init_field + _pad (taufactor.py:282-291, :228-238),
+ * Solver/PeriodicSolver/AnisotropicSolver.init_conductive_neighbours (:402-410, :493-499,
+ * :459-471), the label map of MultiPhaseSolver.init_conductive_neighbours (:585-592) and the
+ * chequerboard (:218-225; colour is taken from the voxel index instead).
+ *   phase_dev   uint8 [batch][nx][ny][nz] (natural layout). binary/anisotropic: 1 = conductive,
+ *               0 = not; multiphase: phase index 1..n_phases.
+ *   profile_dev float [nx] initial value of a conductive voxel in plane x.
+ *   code_dev    uint8 [code_bytes]: binary = neighbour count (0 = frozen), anisotropic =
+ *               neighbour pattern index into op->divisor, multiphase = phase index.
+ *   field_dev   float [field_elems]. Ghost cells are filled too. */
+int tf_pack(const tf_geom* g, const tf_operator* op, const uint8_t* phase_dev,
+            const float* profile_dev, uint8_t* code_dev, float* field_dev, void* stream);
+
+/* Advance the solve by n_half half-sweeps (one colour each), colour of the first one =
+ * first_colour (reference: iter % 2). Replaces the loop body of SORSolver.solve
+ * (taufactor.py:174-182) with sum_weighted_neighbours (:95-103, :473-478, :606-613) and the
+ * periodic ghost copies (:501-505, :652-656), repeated n_half times.
+ * Fields ping-pong between field_a_dev and field_b_dev; *result_in_b is set to 1 when the
+ * result is in field_b_dev, 0 when in field_a_dev (the input must be in field_a_dev).
+ * err_dev (int32, may be NULL) receives TF_ERR_TIMEOUT if a bounded device wait ran out. */
+int tf_advance(const tf_geom* g, const tf_operator* op, float* field_a_dev, float* field_b_dev,
+               const uint8_t* code_dev, int first_colour, int n_half, int32_t* err_dev,
+               int* result_in_b, void* stream);
+
+/* Per-layer float64 sums (not means) for the convergence metrics. Replaces
+ * Solver.vertical_flux / MultiPhaseSolver.vertical_flux (taufactor.py:412-419, :615-620) with
+ * torch.mean(..., (2, 3)) (:296) and the c_x mean (:307).
+ *   flux_sum_dev double [batch][nx-1]: sum over (y, z) of the x-flux through face x|x+1
+ *   c_sum_dev    double [batch][nx]:   sum over (y, z) of the field in plane x  */
+int tf_layer_sums(const tf_geom* g, const tf_operator* op, const float* field_dev,
+                  const uint8_t* code_dev, double* flux_sum_dev, double* c_sum_dev, void* stream);
+
+/* Write the reference's padded field layout float [batch][nx+2][ny+2][nz+2]
+ * (SORSolver.field, taufactor.py:43, padding :228-238): interior from field_dev, x ghost planes
+ * 2*bc, y/z ghosts 0 or (periodic) the wrapped interior. */
+int tf_unpack(const tf_geom* g, const tf_operator* op, const float* field_dev, float* padded_dev,
+              void* stream);
+
+/* Inverse of tf_unpack for the interior: load a padded reference-layout field into field_dev
+ * (ghost cells are rebuilt). Used to resume from a user-supplied field. */
+int tf_repack(const tf_geom* g, const tf_operator* op, const float* padded_dev, float* field_dev,
+              void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TAUFACTOR_GB300_H */

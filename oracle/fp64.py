@@ -1,0 +1,147 @@
+"""FP64 "truth" for the through-transport solve (test infrastructure only).
+
+Assembles, in scipy.sparse, the same discrete operator that the reference's SOR iteration
+converges to (tldr-group/taufactor v1.2.1, taufactor/taufactor.py):
+
+* unknowns: voxels with a finite diagonal (conductive voxels for the binary solvers,
+  ``factor < inf`` for the multiphase ones; :402-410, :598-603);
+* face conductance 1 between two conductive voxels (binary, :95-103), (dx/dy)^2 and (dx/dz)^2
+  on y and z faces (anisotropic, :455-478), the harmonic mean 2ab/(a+b) of the two voxel
+  diffusivities (multiphase, :577-596); y and z faces wrap for the periodic solvers (:493-505,
+  :626-656);
+* Dirichlet inlet/outlet: a voxel on x = 0 (x = Nx-1) couples to the boundary value -0.5
+  (+0.5) with twice its boundary-face conductance, because the boundary sits half a voxel away
+  (the 2 in the padding of :404 and the extra D_x term of :601-602).
+
+Voxels of clusters that touch neither Dirichlet face make the operator singular; they carry no
+flux at convergence, so they are removed (pinned to 0). The system is solved with
+Jacobi-preconditioned CG to a relative residual of 1e-10, and D_eff is formed with the
+reference's layer-flux formula (:293-303, :412-419, :615-620) in float64.
+"""
+from __future__ import annotations
+
+import numpy as np
+import scipy.sparse as sp
+from scipy.sparse.csgraph import connected_components
+from scipy.sparse.linalg import cg
+
+from .sor import OracleSolve
+
+
+def _face_weights(o: OracleSolve):
+    """Conductances of the +x, +y, +z faces of every voxel, [B,X,Y,Z] float64 each.
+
+    The last y/z face wraps to index 0 for periodic solvers and is 0 otherwise; the last x
+    face (outlet) is handled as a Dirichlet term, so its entry here is 0.
+    """
+    B, X, Y, Z = o.batch_size, o.Nx, o.Ny, o.Nz
+    if o.multiphase:
+        gx = np.zeros((B, X, Y, Z))
+        gx[:, :-1] = o.D_x[:, 1:-1]
+        if o.periodic:
+            gy = o.D_y[:, :, 1:].astype(np.float64)
+            gz = o.D_z[:, :, :, 1:].astype(np.float64)
+        else:
+            gy = np.zeros((B, X, Y, Z))
+            gy[:, :, :-1] = o.D_y[:, :, 1:-1]
+            gz = np.zeros((B, X, Y, Z))
+            gz[:, :, :, :-1] = o.D_z[:, :, :, 1:-1]
+        gb_lo = o.D_x[:, 0].astype(np.float64)
+        gb_hi = o.D_x[:, -1].astype(np.float64)
+        return gx, gy, gz, gb_lo, gb_hi
+    m = o.mask.astype(np.float64)
+    ky = getattr(o, "Ky", 1.0)
+    kz = getattr(o, "Kz", 1.0)
+    gx = np.zeros_like(m)
+    gx[:, :-1] = m[:, :-1] * m[:, 1:]
+    if o.periodic:
+        gy = m * np.roll(m, -1, axis=2) * ky
+        gz = m * np.roll(m, -1, axis=3) * kz
+    else:
+        gy = np.zeros_like(m)
+        gy[:, :, :-1] = m[:, :, :-1] * m[:, :, 1:] * ky
+        gz = np.zeros_like(m)
+        gz[:, :, :, :-1] = m[:, :, :, :-1] * m[:, :, :, 1:] * kz
+    return gx, gy, gz, m[:, 0], m[:, -1]
+
+
+def assemble(o: OracleSolve, b: int):
+    """Sparse SPD system (A, rhs, index map) of batch element b."""
+    X, Y, Z = o.Nx, o.Ny, o.Nz
+    gx, gy, gz, gb_lo, gb_hi = (a[b] for a in _face_weights(o))
+    n = X * Y * Z
+    idx = np.arange(n).reshape(X, Y, Z)
+    rows, cols, vals = [], [], []
+    diag = np.zeros(n)
+    for g, nb in ((gx, np.roll(idx, -1, 0)), (gy, np.roll(idx, -1, 1)), (gz, np.roll(idx, -1, 2))):
+        sel = g.ravel() > 0
+        u = idx.ravel()[sel]
+        v = nb.ravel()[sel]
+        w = g.ravel()[sel]
+        rows += [u, v]
+        cols += [v, u]
+        vals += [-w, -w]
+        np.add.at(diag, u, w)
+        np.add.at(diag, v, w)
+    rhs = np.zeros(n)
+    lo = idx[0].ravel()
+    hi = idx[-1].ravel()
+    diag[lo] += 2 * gb_lo.ravel()
+    rhs[lo] += 2 * gb_lo.ravel() * o.top_bc
+    diag[hi] += 2 * gb_hi.ravel()
+    rhs[hi] += 2 * gb_hi.ravel() * o.bot_bc
+    off = sp.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                        shape=(n, n))
+    # keep only clusters that touch a Dirichlet face
+    active = diag > 0
+    dirichlet = np.zeros(n, dtype=bool)
+    dirichlet[lo] |= gb_lo.ravel() > 0
+    dirichlet[hi] |= gb_hi.ravel() > 0
+    ncomp, comp = connected_components(off, directed=False)
+    anchored = np.zeros(ncomp, dtype=bool)
+    anchored[comp[dirichlet]] = True
+    keep = active & anchored[comp]
+    A = (off + sp.diags(diag)).tocsr()
+    k = np.nonzero(keep)[0]
+    return A[k][:, k].tocsr(), rhs[k], k
+
+
+def solve_fp64(o: OracleSolve, rtol: float = 1e-10, maxiter: int = 200000):
+    """FP64 field [B,X,Y,Z] (0 outside anchored clusters) and the CG residuals reached."""
+    B, X, Y, Z = o.batch_size, o.Nx, o.Ny, o.Nz
+    field = np.zeros((B, X, Y, Z))
+    resid = np.zeros(B)
+    prof = np.linspace(o.top_bc + 0.5 / X, o.bot_bc - 0.5 / X, X)
+    for b in range(B):
+        A, rhs, k = assemble(o, b)
+        if len(k) == 0:
+            continue
+        x0 = np.broadcast_to(prof[:, None, None], (X, Y, Z)).ravel()[k]
+        dinv = 1.0 / A.diagonal()
+        M = sp.diags(dinv)
+        sol, info = cg(A, rhs, x0=x0, rtol=rtol, atol=0.0, maxiter=maxiter, M=M)
+        if info != 0:
+            raise RuntimeError(f"FP64 CG did not reach rtol={rtol} (info={info})")
+        resid[b] = np.linalg.norm(rhs - A @ sol) / max(np.linalg.norm(rhs), 1e-300)
+        f = np.zeros(X * Y * Z)
+        f[k] = sol
+        field[b] = f.reshape(X, Y, Z)
+    return field, resid
+
+
+def layer_flux_fp64(o: OracleSolve, field: np.ndarray) -> np.ndarray:
+    """Reference layer-flux formula (taufactor.py:412-419, :615-620) in float64, [B,X-1]."""
+    d = field[:, 1:] - field[:, :-1]
+    if o.multiphase:
+        return (o.D_x[:, 1:-1].astype(np.float64) * d).mean(axis=(2, 3))
+    fin = np.isfinite(o.factor)
+    d = d * (fin[:, :-1] & fin[:, 1:])
+    return d.mean(axis=(2, 3))
+
+
+def d_eff_fp64(o: OracleSolve, rtol: float = 1e-10):
+    """FP64 D_eff per batch element (D_0 * mean layer flux * Nx / |bc difference|)."""
+    field, resid = solve_fp64(o, rtol=rtol)
+    flux = layer_flux_fp64(o, field)
+    d_rel = flux.mean(axis=1) * o.Nx / abs(o.top_bc - o.bot_bc)
+    return o.D_0 * d_rel, field, resid

@@ -1,0 +1,44 @@
+"""Import the reference package from its source tree (test infrastructure only).
+
+The reference (tldr-group/taufactor v1.2.1) imports IPython, matplotlib and scikit-image at
+module level for plotting and surface metrics; none of them is used on the solve path unless
+``verbose='plot'|'debug'``. Stub modules stand in for them. Bytecode writing is disabled so the
+read-only source tree is left untouched.
+
+Only the golden-vector generator and the CPU oracle tests use this, and only where the source
+tree exists (``TAUFACTOR_REFERENCE`` or the default location below); it never runs on the GPU
+machine.
+"""
+from __future__ import annotations
+
+import os
+import sys
+import types
+
+DEFAULT_REFERENCE = "/root/reference"
+
+
+def reference_root() -> str | None:
+    root = os.environ.get("TAUFACTOR_REFERENCE", DEFAULT_REFERENCE)
+    return root if os.path.isdir(os.path.join(root, "taufactor")) else None
+
+
+def import_reference():
+    """Return the reference ``taufactor`` module, or None if its source tree is absent."""
+    root = reference_root()
+    if root is None:
+        return None
+    sys.dont_write_bytecode = True
+    for name in ("IPython", "IPython.display", "matplotlib", "matplotlib.pyplot",
+                 "skimage", "skimage.measure"):
+        if name not in sys.modules:
+            sys.modules[name] = types.ModuleType(name)
+    sys.modules["IPython.display"].clear_output = lambda *a, **k: None
+    sys.modules["IPython"].display = sys.modules["IPython.display"]
+    sys.modules["matplotlib"].pyplot = sys.modules["matplotlib.pyplot"]
+    sys.modules["skimage"].measure = sys.modules["skimage.measure"]
+    if root not in sys.path:
+        sys.path.insert(0, root)
+    import taufactor  # noqa: E402
+
+    return taufactor

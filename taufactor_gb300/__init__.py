@@ -1,0 +1,14 @@
+"""taufactor_gb300: TauFactor's steady-state voxel diffusion solve on one GB300 (sm_103a).
+
+Drop-in for the through-transport solvers of tldr-group/taufactor v1.2.1
+(``taufactor/__init__.py:3-11``): ``Solver``, ``PeriodicSolver``, ``AnisotropicSolver``,
+``MultiPhaseSolver`` and ``PeriodicMultiPhaseSolver`` with the same constructor and ``solve()``
+surface. The sweeps run as hand-written CUDA kernels of ``lib/libtaufactor_gb300.so`` through
+its C ABI (``include/taufactor_gb300.h``).
+"""
+from .solvers import (AnisotropicSolver, MultiPhaseSolver, PeriodicMultiPhaseSolver, PeriodicSolver,
+                      SORSolver, Solver, ThroughTransportSolver)
+
+__all__ = ["Solver", "PeriodicSolver", "AnisotropicSolver", "MultiPhaseSolver", "PeriodicMultiPhaseSolver",
+           "SORSolver", "ThroughTransportSolver"]
+__version__ = "0.1.0"

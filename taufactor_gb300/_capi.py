@@ -1,0 +1,96 @@
+"""ctypes binding of libtaufactor_gb300.so (the C ABI declared in include/taufactor_gb300.h).
+
+The library is built in-tree by ``taufactor_gb300.build`` (``__graft_entry__.build()``). If it
+is missing, or no CUDA device is present, the solvers raise: there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+_LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "libtaufactor_gb300.so")
+
+TF_OK, TF_ERR_ARG, TF_ERR_CUDA, TF_ERR_TIMEOUT, TF_ERR_UNSUPPORTED, TF_ERR_NOTCONV = range(6)
+TF_KIND_BINARY, TF_KIND_ANISOTROPIC, TF_KIND_MULTIPHASE = 0, 1, 2
+TF_PERIODIC_Y, TF_PERIODIC_Z = 1, 2
+TF_MAX_PHASES = 31
+TF_MAX_HALF_SWEEPS = 4
+
+# every symbol the header declares (checked by the CPU tests)
+EXPORTS = (
+    "tf_version", "tf_status_string", "tf_launch_count", "tf_geometry", "tf_pack", "tf_advance",
+    "tf_layer_sums", "tf_unpack", "tf_repack",
+)
+
+
+class TfGeom(C.Structure):
+    _fields_ = [("batch", C.c_int32), ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
+                ("halo_y", C.c_int32), ("halo_j", C.c_int32), ("yp", C.c_int32), ("zh", C.c_int32),
+                ("zhc", C.c_int32), ("tiled", C.c_int32), ("field_elems", C.c_int64),
+                ("code_bytes", C.c_int64)]
+
+
+class TfOperator(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("periodic", C.c_int32), ("omega", C.c_float),
+                ("ghost_lo", C.c_float), ("ghost_hi", C.c_float), ("ky", C.c_float), ("kz", C.c_float),
+                ("n_phases", C.c_int32), ("divisor", C.c_float * 256), ("face", C.c_float * 1024),
+                ("conductive", C.c_uint8 * 32)]
+
+
+class TfError(RuntimeError):
+    """A taufactor_gb300 C-ABI call returned a non-zero status."""
+
+    def __init__(self, status: int, what: str):
+        self.status = status
+        super().__init__(f"{what} failed: {status_string(status)} (status {status})")
+
+
+_lib = None
+
+
+def lib_path() -> str:
+    return _LIB_PATH
+
+
+def load():
+    """Load the shared library (once); raises ImportError with a build hint if absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(_LIB_PATH):
+        raise ImportError(f"{_LIB_PATH} is missing: build it with "
+                          "`python -m taufactor_gb300.build` (needs nvcc)")
+    L = C.CDLL(_LIB_PATH)
+    vp, i32, i64 = C.c_void_p, C.c_int, C.c_int64
+    G, O = C.POINTER(TfGeom), C.POINTER(TfOperator)
+    sig = {
+        "tf_version": (C.c_char_p, []),
+        "tf_status_string": (C.c_char_p, [i32]),
+        "tf_launch_count": (i64, []),
+        "tf_geometry": (i32, [i32, i32, i32, i32, i32, G]),
+        "tf_pack": (i32, [G, O, vp, vp, vp, vp, vp]),
+        "tf_advance": (i32, [G, O, vp, vp, vp, i32, i32, vp, C.POINTER(C.c_int), vp]),
+        "tf_layer_sums": (i32, [G, O, vp, vp, vp, vp, vp]),
+        "tf_unpack": (i32, [G, O, vp, vp, vp]),
+        "tf_repack": (i32, [G, O, vp, vp, vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def status_string(status: int) -> str:
+    try:
+        return load().tf_status_string(status).decode()
+    except ImportError:
+        return f"status {status}"
+
+
+def check(status: int, what: str) -> None:
+    if status != TF_OK:
+        if status == TF_ERR_ARG:
+            raise ValueError(f"{what}: invalid argument (status {status})")
+        raise TfError(status, what)

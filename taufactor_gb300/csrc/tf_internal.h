@@ -1,0 +1,35 @@
+// Internal host-side interface between the translation units of libtaufactor_gb300.
+#pragma once
+
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/taufactor_gb300.h"
+
+namespace tf {
+
+constexpr int TILE_Y = 16;  // tile rows (y) of the tiled sweep
+constexpr int TILE_Z = 64;  // tile columns (z) of the tiled sweep (multiple of 32)
+
+void note_launch();
+
+// 3-D tiled tensor map over [dim2][dim1][dim0] with the given byte strides of dims 1 and 2.
+int encode_map_3d(CUtensorMap* map, const void* base, int elem_bytes, long long dim0, long long dim1,
+                  long long dim2, long long stride1_bytes, long long stride2_bytes, int box0, int box1);
+
+int sweep_tiled(const tf_geom& g, const tf_operator& op, const float* in, float* out, const uint8_t* code,
+                int first_colour, int n_half, int32_t* err, cudaStream_t st);
+int sweep_plain(const tf_geom& g, const tf_operator& op, float* f, const uint8_t* code, int colour,
+                cudaStream_t st);
+int refresh_ghosts(const tf_geom& g, int periodic, float* f, cudaStream_t st);
+int tiled_smem_bytes();
+
+int pack(const tf_geom& g, const tf_operator& op, const uint8_t* phase, const float* profile, uint8_t* code,
+         float* field, cudaStream_t st);
+int unpack(const tf_geom& g, const tf_operator& op, const float* field, float* padded, cudaStream_t st);
+int repack(const tf_geom& g, const tf_operator& op, const float* padded, float* field, cudaStream_t st);
+int layer_sums(const tf_geom& g, const tf_operator& op, const float* field, const uint8_t* code, double* flux,
+               double* csum, cudaStream_t st);
+
+}  // namespace tf

@@ -1,0 +1,484 @@
+"""Drop-in solver classes for TauFactor's through-transport solve on one GB300.
+
+Mirrors the reference's operator surface (tldr-group/taufactor v1.2.1,
+taufactor/taufactor.py): the class names, constructor arguments, ``solve()`` arguments and
+return value, the attributes it sets (``tau``, ``D_eff``, ``tau_x``, ``c_x``, ``flux_1d``,
+``vol_x``, ``D_mean``, ``D_0``, ``iter``, ``converged``, ``walltime``, ``field``), its errors and
+warnings, and its convergence rule (layer-flux spread and tau change, checked every 100
+half-sweeps). The half-sweeps themselves, the set-up and the layer reductions run as sm_103a
+kernels of libtaufactor_gb300 through its C ABI; each half-sweep is the reference's
+arithmetic bit for bit.
+
+Deliberate differences:
+* a non-CUDA device raises RuntimeError (the reference warns and falls back to the CPU,
+  :207-216): there is no CPU path;
+* layer means are accumulated in float64 on the device (the reference reduces in float32), so
+  ``flux_1d``, ``c_x``, ``tau`` and ``D_eff`` are float64 arrays;
+* ``field`` is assembled on access in the reference's padded layout; the solver keeps the
+  volume in a z-parity split layout on the device.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import warnings
+from timeit import default_timer as timer
+
+import numpy as np
+import torch
+
+from . import _capi
+from ._capi import (TF_KIND_ANISOTROPIC, TF_KIND_BINARY, TF_KIND_MULTIPHASE, TF_MAX_PHASES,
+                    TF_PERIODIC_Y, TF_PERIODIC_Z, TfGeom, TfOperator, check)
+from .percolation import spans_x
+
+F32 = np.float32
+INF32 = F32(np.inf)
+
+
+def _ptr(t: torch.Tensor) -> int:
+    return t.data_ptr()
+
+
+class SORSolver:
+    """Template of the red-black SOR solve (taufactor.py:15-269).
+
+    Subclasses define the conductive mask / phase indices and the operator; this class owns
+    the device buffers, the half-sweep loop and the convergence checks.
+    """
+
+    _kind = TF_KIND_BINARY
+    _periodic = 0
+    #: set to a list to record (start event, end event, half-sweeps) around every tf_advance call
+    event_log = None
+
+    def __init__(self, img: np.ndarray, omega: float | None = None, precision=None, device="cuda"):
+        self.cpu_img = self._expand_to_4d(img)
+        self.batch_size, self.Nx, self.Ny, self.Nz = self.cpu_img.shape
+        self.device = self._init_device(device)
+        if precision not in (None, torch.float32):
+            raise ValueError("taufactor_gb300 sweeps in float32; precision must be None or torch.float32")
+        self.precision = torch.float32
+        if omega is None:
+            omega = 2 - math.pi / (1.5 * self.Nx)  # taufactor.py:36-37
+        self.omega = omega
+        phase, mask = self._phase_indices()
+        self.vol_x = mask.mean(axis=(2, 3), dtype=np.float64)
+        self._op = self._operator(float(omega))
+        self._build(phase)
+        self.converged = False
+        self.old_tau = 0
+        self.iter = 0
+        self.tau = None
+        self.tau_x = None
+        self.D_eff = None
+        self.walltime = 0.0
+
+    # ------------------------------------------------------------------ hooks
+    def _phase_indices(self):
+        """uint8 phase indices [B,X,Y,Z] for tf_pack and the bool conductive mask."""
+        raise NotImplementedError
+
+    def _operator(self, omega: float) -> TfOperator:
+        op = TfOperator()
+        op.kind = self._kind
+        op.periodic = self._periodic
+        op.omega = float(F32(omega))
+        op.ghost_lo = 2 * self.top_bc
+        op.ghost_hi = 2 * self.bot_bc
+        op.ky = op.kz = 1.0
+        for i in range(256):
+            op.divisor[i] = np.inf
+        return op
+
+    # ------------------------------------------------------------------ device state
+    def _build(self, phase: np.ndarray):
+        self._lib = _capi.load()
+        g = TfGeom()
+        check(self._lib.tf_geometry(self.batch_size, self.Nx, self.Ny, self.Nz, self._periodic, C.byref(g)),
+              "tf_geometry")
+        self._geom = g
+        dev = self.device
+        with torch.cuda.device(dev):
+            self._code = torch.empty(g.code_bytes, dtype=torch.uint8, device=dev)
+            self._fa = torch.empty(g.field_elems, dtype=torch.float32, device=dev)
+            self._fb = torch.zeros(g.field_elems, dtype=torch.float32, device=dev)
+            self._err = torch.zeros(1, dtype=torch.int32, device=dev)
+            sh = 1 / (2 * self.Nx)
+            # the reference's float32 linspace (taufactor.py:284-286), computed on the host
+            profile = torch.linspace(self.top_bc + sh, self.bot_bc - sh, self.Nx, dtype=torch.float32).to(dev)
+            phase_dev = torch.from_numpy(np.ascontiguousarray(phase, dtype=np.uint8)).to(dev)
+            self._phase_dev, self._profile_dev = phase_dev, profile
+            self._pack()
+            self._flux_dev = torch.empty((self.batch_size, max(self.Nx - 1, 1)), dtype=torch.float64, device=dev)
+            self._csum_dev = torch.empty((self.batch_size, self.Nx), dtype=torch.float64, device=dev)
+        self._cur, self._other = self._fa, self._fb
+
+    def _pack(self):
+        with torch.cuda.device(self.device):
+            check(self._lib.tf_pack(C.byref(self._geom), C.byref(self._op), _ptr(self._phase_dev),
+                                    _ptr(self._profile_dev), _ptr(self._code), _ptr(self._fa), self._stream()),
+                  "tf_pack")
+
+    def reset(self):
+        """Restart the solve from the initial linear field, keeping the device buffers."""
+        self._pack()
+        self._cur, self._other = self._fa, self._fb
+        self.converged = False
+        self.old_tau = 0
+        self.iter = 0
+        self.tau = self.tau_x = self.D_eff = None
+
+    def _stream(self):
+        return torch.cuda.current_stream(self.device).cuda_stream
+
+    def _advance(self, n: int):
+        """n half-sweeps (reference iterations) starting at colour iter % 2."""
+        if n <= 0:
+            return
+        in_b = C.c_int(0)
+        ev = self.event_log
+        if ev is not None:
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record()
+        with torch.cuda.device(self.device):
+            check(self._lib.tf_advance(C.byref(self._geom), C.byref(self._op), _ptr(self._cur), _ptr(self._other),
+                                       _ptr(self._code), self.iter % 2, n, _ptr(self._err), C.byref(in_b),
+                                       self._stream()), "tf_advance")
+        if ev is not None:
+            e1.record()
+            ev.append((e0, e1, n))
+        if in_b.value:
+            self._cur, self._other = self._other, self._cur
+        self.iter += n
+
+    def _layer_means(self):
+        """float64 per-layer means of the x-flux [B,Nx-1] and of the field [B,Nx]."""
+        with torch.cuda.device(self.device):
+            check(self._lib.tf_layer_sums(C.byref(self._geom), C.byref(self._op), _ptr(self._cur), _ptr(self._code),
+                                          _ptr(self._flux_dev), _ptr(self._csum_dev), self._stream()),
+                  "tf_layer_sums")
+            flux = self._flux_dev.cpu().numpy()
+            csum = self._csum_dev.cpu().numpy()
+            err = int(self._err.item())
+        if err:
+            self._err.zero_()
+            raise _capi.TfError(err, "tf_advance (device)")
+        area = float(self.Ny * self.Nz)
+        return flux[:, : self.Nx - 1] / area, csum / area
+
+    @property
+    def field(self) -> torch.Tensor:
+        """The concentration field in the reference's padded layout [B,Nx+2,Ny+2,Nz+2] (a copy)."""
+        out = torch.empty((self.batch_size, self.Nx + 2, self.Ny + 2, self.Nz + 2), dtype=torch.float32,
+                          device=self.device)
+        with torch.cuda.device(self.device):
+            check(self._lib.tf_unpack(C.byref(self._geom), C.byref(self._op), _ptr(self._cur), _ptr(out),
+                                      self._stream()), "tf_unpack")
+        return out
+
+    @field.setter
+    def field(self, value: torch.Tensor):
+        shape = (self.batch_size, self.Nx + 2, self.Ny + 2, self.Nz + 2)
+        v = torch.as_tensor(value, dtype=torch.float32, device=self.device).reshape(shape).contiguous()
+        with torch.cuda.device(self.device):
+            check(self._lib.tf_repack(C.byref(self._geom), C.byref(self._op), _ptr(v), _ptr(self._cur),
+                                      self._stream()), "tf_repack")
+
+    # ------------------------------------------------------------------ convergence
+    def compute_metrics(self):
+        raise NotImplementedError
+
+    def plot_stats(self, relative_error):
+        """Headless stand-in for the reference's matplotlib plot (taufactor.py:333-352)."""
+        i = int(np.argmax(relative_error))
+        print(f"Iter: {self.iter}, conv error: {abs(relative_error[i]):.3E}, tau: {self.tau[i]:.5f} "
+              f"(batch element {i})")
+
+    def check_convergence(self, verbose, conv_crit, plot_interval):
+        """taufactor.py:109-153."""
+        self.tau, relative_error = self.compute_metrics()
+        if verbose == "per_iter":
+            i = int(np.argmax(relative_error))
+            print(f"Iter: {self.iter}, conv error: {abs(relative_error[i]):.3E}, tau: {self.tau[i]:.5f} "
+                  f"(batch element {i})")
+        if verbose == "plot" and self.iter % (100 * plot_interval) == 0:
+            self.plot_stats(relative_error)
+        if verbose == "debug":
+            self.tau_t.append(self.tau)
+            if self.iter % (100 * plot_interval) == 0:
+                i = int(np.argmax(np.abs(relative_error)))
+                print(f"Iter: {self.iter}, conv error: {np.abs(relative_error[i]):.3E}, tau: {self.tau[i]:.5f} "
+                      f"(batch element {i})")
+        if not np.all(relative_error < conv_crit):
+            self.old_tau = self.tau
+            return False
+        tau_error = np.max(np.abs(self.tau - self.old_tau))
+        if not tau_error < 2e-3:
+            self.old_tau = self.tau
+            return False
+        self.tau[self.tau == 0] = np.inf
+        return True
+
+    def solve(self, iter_limit=10000, verbose=True, conv_crit=1e-2, plot_interval=10):
+        """Run half-sweeps until converged or iter_limit (taufactor.py:156-191).
+
+        Half-sweeps between two checks run as fused multi-half-sweep launches with no host
+        synchronisation; the check every 100 half-sweeps reads the layer sums back.
+        """
+        if verbose:
+            torch.cuda.reset_peak_memory_stats(device=self.device)
+        if verbose == "debug":
+            self.tau_t = []
+        start = timer()
+        while not self.converged and self.iter < iter_limit:
+            n = min(100 - self.iter % 100, iter_limit - self.iter)
+            self._advance(n)
+            if self.iter % 100 == 0:
+                self.converged = self.check_convergence(verbose, conv_crit, plot_interval)
+        torch.cuda.synchronize(self.device)
+        self.walltime = timer() - start
+        self._end_simulation(self.iter, verbose)
+        if self.tau_x is None:
+            return self.tau
+        return self.tau_x
+
+    # ------------------------------------------------------------------ helpers
+    @staticmethod
+    def _expand_to_4d(img) -> np.ndarray:
+        """taufactor.py:195-204."""
+        if not isinstance(img, np.ndarray):
+            raise TypeError("Error: input image must be a NumPy array!")
+        if img.ndim == 2:
+            img = img[..., None]
+        if img.ndim == 3:
+            img = img[None, ...]
+        if img.ndim != 4:
+            raise ValueError("expected [B, X, Y, Z]")
+        return img
+
+    @staticmethod
+    def _init_device(device) -> torch.device:
+        """CUDA only: the reference's CPU fallback (taufactor.py:207-216) becomes an error."""
+        dev = torch.device(device)
+        if dev.type != "cuda":
+            raise RuntimeError(f"taufactor_gb300 runs on CUDA devices only (got device={device!r}); "
+                               "use the reference package for CPU solves")
+        if not torch.cuda.is_available():
+            raise RuntimeError("taufactor_gb300 needs a CUDA device, and none is available")
+        if dev.index is None:
+            dev = torch.device("cuda", torch.cuda.current_device())
+        return dev
+
+    def _end_simulation(self, iterations: int, verbose):
+        """taufactor.py:255-269."""
+        if self.converged:
+            msg = "converged to"
+        else:
+            print("Warning: not converged")
+            msg = "unconverged value of tau"
+        if verbose:
+            per = self.walltime / iterations if iterations else 0.0
+            print(f"{msg}: {self.tau} after: {iterations} iterations in: {np.around(self.walltime, 4)} s "
+                  f"({np.around(per, 4)} s/iter)")
+            print(f"GPU-RAM currently {torch.cuda.memory_allocated(device=self.device) / 1e6:.2f} MB "
+                  f"(max allocated {torch.cuda.max_memory_allocated(device=self.device) / 1e6:.2f} MB; "
+                  f"{torch.cuda.max_memory_reserved(device=self.device) / 1e6:.2f} MB reserved)")
+
+
+class ThroughTransportSolver(SORSolver):
+    """Dirichlet x-faces at (-0.5, 0.5), flux-based metrics (taufactor.py:272-331)."""
+
+    def __init__(self, img, omega=None, precision=None, device="cuda"):
+        self.top_bc, self.bot_bc = (-0.5, 0.5)
+        super().__init__(img, omega, precision, device)
+
+    def compute_metrics(self):
+        """taufactor.py:293-331 on float64 layer means read back from the device."""
+        self.flux_1d, c_x = self._layer_means()
+        fl_max = np.max(self.flux_1d, axis=1)
+        fl_min = np.min(self.flux_1d, axis=1)
+        mean_fl = np.mean(self.flux_1d, axis=1)
+        relative_error = np.divide(fl_max - fl_min, fl_max, out=np.full_like(fl_max, np.nan), where=fl_max != 0)
+        D_rel = mean_fl * self.Nx / abs(self.top_bc - self.bot_bc)
+        tau = np.divide(self.D_mean, D_rel, out=np.full_like(D_rel, np.nan), where=D_rel != 0)
+        c_x = np.divide(c_x, self.vol_x, out=np.zeros_like(self.vol_x), where=self.vol_x != 0)
+        self.c_x = c_x
+        flux_from_c = c_x[:, 1:] - c_x[:, :-1]
+        flux_from_c[self.vol_x[:, 1:] == 0] = 0
+        flux_from_c[self.vol_x[:, :-1] == 0] = 0
+        eps = 0.5 * (self.vol_x[:, :-1] + self.vol_x[:, 1:])
+        self.tau_x = np.divide(eps * flux_from_c, self.flux_1d, out=np.full_like(flux_from_c, np.nan),
+                               where=self.flux_1d != 0)
+        for b in range(self.batch_size):
+            if (fl_min[b] == 0) or (fl_max[b] == 0) or (mean_fl[b] == 0):
+                if not spans_x(np.isin(self.cpu_img[b], self.conductive_labels)):
+                    print(f"Warning: batch element {b} has no percolating path!")
+                    relative_error[b] = 0
+                    D_rel[b] = 0
+                    tau[b] = 0
+                    self.tau_x[b, :] = 0
+        relative_error[np.isnan(mean_fl)] = 0
+        self.D_eff = self.D_0 * D_rel
+        return tau, relative_error
+
+
+class Solver(ThroughTransportSolver):
+    """Two-phase solver: 1 = conductive, 0 = not (taufactor.py:355-419)."""
+
+    def __init__(self, img, omega=None, D_0=1, device="cuda"):
+        self._check_binary_labels(img)
+        self.conductive_labels = [1]
+        super().__init__(img, omega=omega, device=device)
+        self.D_0 = D_0
+        self.D_mean = np.mean(self.vol_x, axis=1)
+
+    def _check_binary_labels(self, img):
+        """taufactor.py:387-397 (same message)."""
+        u = np.unique(img)
+        if len(u) > 2 or u.max() not in [0, 1] or u.min() not in [0, 1]:
+            raise ValueError(
+                "Input image must only contain 0s and 1s. "
+                "Your image must be segmented to use this tool. "
+                "If your image has been segmented, ensure your labels are "
+                "0 for non-conductive and 1 for conductive phase. "
+                f"Your image has the following labels: {u}. "
+                "If you have more than one conductive phase, use the multi-phase solver.")
+
+    def _phase_indices(self):
+        mask = self.cpu_img == 1
+        return mask.astype(np.uint8), mask
+
+    def _operator(self, omega):
+        op = super()._operator(omega)
+        for n in range(1, 9):
+            op.divisor[n] = float(n)
+        return op
+
+
+class PeriodicSolver(Solver):
+    """Two-phase solver, periodic in y and z (taufactor.py:481-505)."""
+
+    _periodic = TF_PERIODIC_Y | TF_PERIODIC_Z
+
+
+def anisotropic_divisors(ky: float, kz: float) -> np.ndarray:
+    """float32 diagonal of every neighbour pattern, in the reference's summation order.
+
+    Pattern index 1 + xm + 3 xp + 9 ym + 18 yp + 36 zm + 72 zp (xm, xp in {0,1,2}: 2 = Dirichlet
+    face; others in {0,1}); index 0 = non-conductive. AnisotropicSolver.init_conductive_neighbours
+    (taufactor.py:459-471) accumulates x-1, x+1, y-1, y+1, z-1, z+1, each times its weight.
+    """
+    out = np.full(256, np.inf, dtype=F32)
+    w = (F32(1.0), F32(1.0), F32(ky), F32(ky), F32(kz), F32(kz))
+    for xm in range(3):
+        for xp in range(3):
+            for ym in range(2):
+                for yp in range(2):
+                    for zm in range(2):
+                        for zp in range(2):
+                            s = F32(0)
+                            for m, wt in zip((xm, xp, ym, yp, zm, zp), w):
+                                s = F32(s + F32(F32(m) * wt))
+                            idx = 1 + xm + 3 * xp + 9 * ym + 18 * yp + 36 * zm + 72 * zp
+                            out[idx] = s if s != 0 else INF32
+    return out
+
+
+class AnisotropicSolver(Solver):
+    """Binary solver with voxel spacing (dx, dy, dz) (taufactor.py:422-478)."""
+
+    _kind = TF_KIND_ANISOTROPIC
+
+    def __init__(self, img, spacing, omega=None, D_0=1, device="cuda:0"):
+        if not isinstance(spacing, (list, tuple)) or len(spacing) != 3:
+            raise ValueError("spacing must be a list or tuple with three elements (dx, dy, dz)")
+        if not all(isinstance(x, (int, float)) for x in spacing):
+            raise ValueError("All elements in spacing must be integers or floats")
+        if np.max(spacing) / np.min(spacing) > 10:
+            warnings.warn("This computation is very questionable for largely different spacings e.g. dz >> dx.")
+        dx, dy, dz = spacing
+        self.Ky = (dx / dy) ** 2
+        self.Kz = (dx / dz) ** 2
+        super().__init__(img, omega=omega, D_0=D_0, device=device)
+
+    def _operator(self, omega):
+        op = SORSolver._operator(self, omega)
+        op.ky = float(F32(self.Ky))
+        op.kz = float(F32(self.Kz))
+        for i, v in enumerate(anisotropic_divisors(self.Ky, self.Kz)):
+            op.divisor[i] = float(v)
+        return op
+
+
+def harmonic_face(a, b) -> F32:
+    """float32 2ab/(a+b), 0 if a+b == 0 (taufactor.py:577-583)."""
+    a, b = F32(a), F32(b)
+    den = F32(a + b)
+    if not den > 0:
+        return F32(0)
+    return F32(F32(F32(F32(2) * a) * b) / den)
+
+
+class MultiPhaseSolver(ThroughTransportSolver):
+    """Per-phase diffusivities with harmonic-mean faces (taufactor.py:508-620)."""
+
+    _kind = TF_KIND_MULTIPHASE
+
+    def __init__(self, img, diffusivities=None, D_scaling=1, omega=None, device="cuda"):
+        if diffusivities is None:
+            diffusivities = {0: 0, 1: 1}
+        if not isinstance(diffusivities, dict):
+            raise TypeError("diffusivities must be a dictionary mapping phase labels to diffusivities")
+        for phase, D_p in diffusivities.items():
+            if not isinstance(phase, (int, np.integer)):
+                raise TypeError(f"Phase label must be integer, got {type(phase).__name__}")
+            D_p = float(D_p)
+            if (not np.isfinite(D_p)) or (D_p < 0):
+                raise ValueError(f"Diffusivity for label {phase} must be finite and >= 0, got {D_p}")
+        self.Ds = diffusivities
+        missing_labels = sorted(int(lbl) for lbl in np.unique(img) if lbl not in self.Ds)
+        if missing_labels:
+            warnings.warn("No diffusivity provided for phase label(s) "
+                          f"{missing_labels}; assuming these phases are isolating.", UserWarning)
+            for lbl in missing_labels:
+                self.Ds[lbl] = 0.0
+        self.conductive_labels = [lbl for lbl, D_p in self.Ds.items() if D_p > 0]
+        super().__init__(img, omega=omega, device=device)
+        self.VF = {int(p): np.mean(self.cpu_img == p, axis=(1, 2, 3)) for p in np.unique(self.cpu_img)}
+        self.D_0 = D_scaling
+        self.D_mean = np.sum([self.VF[z] * self.Ds.get(z, 0.0) for z in self.VF], axis=0)
+
+    def _phase_indices(self):
+        labels = np.unique(self.cpu_img)
+        if len(labels) > TF_MAX_PHASES:
+            raise _capi.TfError(_capi.TF_ERR_UNSUPPORTED,
+                                f"MultiPhaseSolver with {len(labels)} labels (at most {TF_MAX_PHASES})")
+        self._labels = labels
+        idx = np.searchsorted(labels, self.cpu_img).astype(np.uint8) + 1
+        cond = np.isin(self.cpu_img, np.array(self.conductive_labels, dtype=np.float64)) \
+            if self.conductive_labels else np.zeros(self.cpu_img.shape, dtype=bool)
+        return idx, cond
+
+    def _operator(self, omega):
+        op = super()._operator(omega)
+        labels = self._labels
+        op.n_phases = len(labels)
+        d = [F32(0)] + [F32(self.Ds[int(lbl)] if int(lbl) in self.Ds else self.Ds.get(lbl, 0.0))
+                        for lbl in labels]
+        for a in range(32):
+            op.conductive[a] = 0
+            for b in range(32):
+                op.face[a * 32 + b] = 0.0
+        for a in range(len(d)):
+            op.conductive[a] = 1 if (a > 0 and labels[a - 1] in self.conductive_labels) else 0
+            for b in range(len(d)):
+                op.face[a * 32 + b] = float(harmonic_face(d[a], d[b]))
+        return op
+
+
+class PeriodicMultiPhaseSolver(MultiPhaseSolver):
+    """Multiphase, periodic in y and z (taufactor.py:623-656)."""
+
+    _periodic = TF_PERIODIC_Y | TF_PERIODIC_Z

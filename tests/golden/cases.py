@@ -1,0 +1,134 @@
+"""Deterministic inputs of the golden cases.
+
+The solver cases restate the known-answer tests of the reference
+(tldr-group/taufactor v1.2.1, tests/test_taufactor.py; line numbers cited per case) plus the
+100^3 Bernoulli(0.5) workload and a few small random volumes whose field after a fixed number of
+half-sweeps is stored bit for bit. ``make_golden.py`` runs the reference on each input and writes
+``reference_outputs.npz``; the tests rebuild the same inputs from here.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def _slanted(n=20):
+    img = np.zeros((n, n + 1, n + 1))
+    for i in range(n):
+        img[i, i:i + 2, i:i + 2] = 1
+    return img
+
+
+def _blocks(shape):
+    img = np.ones(shape)
+    img[:, 0] = 0
+    return img
+
+
+def _non_percolating(n=20):
+    img = np.zeros((n, n, n))
+    img[:2] = 1
+    return img
+
+
+def _strip(n=20, t=10):
+    img = np.zeros((n, n, n))
+    img[:, 0:t, 0:t] = 1
+    return img
+
+
+def _deadend():
+    img = np.zeros((10, 50, 50))
+    img[:8, 25, 25] = 1
+    return img
+
+
+def _strip12():
+    img = np.zeros((20, 20, 20))
+    img[:, 0:10, 0:10] = 1
+    img[:, 0:10, 10:20] = 2
+    return img
+
+
+def _strip123():
+    img = np.ones((20, 20, 20))
+    img[:, 0:10, 0:10] = 2
+    img[:, 0:10, 10:20] = 3
+    return img
+
+
+def _label0_conductive():
+    img = np.zeros((20, 20, 20))
+    img[:, :2] = 1
+    return img
+
+
+def _batched_mp():
+    a = np.ones((16, 16, 16))
+    b = np.ones((16, 16, 16))
+    b[:, :, :8] = 2
+    return np.stack([a, b], axis=0)
+
+
+def bernoulli_100():
+    """100^3 iid Bernoulli(0.5) voxels from seed 0 (1 = conductive)."""
+    return (np.random.default_rng(0).random((100, 100, 100)) < 0.5).astype(np.uint8)
+
+
+def random_binary(shape, seed, p=0.6):
+    return (np.random.default_rng(seed).random(shape) < p).astype(np.uint8)
+
+
+def random_labels(shape, seed, n=3):
+    return np.random.default_rng(seed).integers(0, n, shape).astype(np.uint8)
+
+
+# name -> (kind, input builder, constructor kwargs, solve kwargs, reference test it restates)
+SOLVE_CASES = {
+    "blocks_cube": ("binary", lambda: _blocks((20, 20, 20)), {}, {}, "test_taufactor.py:12-19"),
+    "blocks_long_x": ("binary", lambda: _blocks((40, 20, 20)), {}, {}, "test_taufactor.py:21-28"),
+    "blocks_long_z": ("binary", lambda: _blocks((20, 20, 40)), {}, {}, "test_taufactor.py:30-37"),
+    "nonperc": ("binary", _non_percolating, {}, {"iter_limit": 1000}, "test_taufactor.py:39-46"),
+    "strip": ("binary", _strip, {}, {}, "test_taufactor.py:48-56"),
+    "slanted": ("binary", _slanted, {}, {}, "test_taufactor.py:58-66"),
+    "deadend": ("binary", _deadend, {}, {}, "test_taufactor.py:68-76"),
+    "p_blocks": ("periodic", lambda: _blocks((20, 20, 20)), {}, {}, "test_taufactor.py:80-87"),
+    "p_nonperc": ("periodic", _non_percolating, {}, {"iter_limit": 1000}, "test_taufactor.py:89-96"),
+    "p_strip": ("periodic", _strip, {}, {}, "test_taufactor.py:98-106"),
+    "p_slanted": ("periodic", _slanted, {}, {"iter_limit": 1000}, "test_taufactor.py:234-247"),
+    "mp_nonperc": ("multiphase", _non_percolating, {}, {"iter_limit": 1000}, "test_taufactor.py:110-117"),
+    "mp_ones": ("multiphase", lambda: np.ones((20, 20, 20)), {}, {"iter_limit": 1000},
+                "test_taufactor.py:119-125"),
+    "mp_halves": ("multiphase", lambda: np.ones((20, 20, 20)), {"diffusivities": {1: 0.5}},
+                  {"iter_limit": 1000}, "test_taufactor.py:127-134"),
+    "mp_strip": ("multiphase", _strip, {}, {}, "test_taufactor.py:136-144"),
+    "mp_strip12": ("multiphase", _strip12, {"diffusivities": {0: 0, 1: 1, 2: 0.5}}, {},
+                   "test_taufactor.py:146-156"),
+    "mp_strip123": ("multiphase", _strip123, {"diffusivities": {0: 0, 1: 1, 2: 0.5, 3: 2}}, {},
+                    "test_taufactor.py:158-168"),
+    "mp_label0": ("multiphase", _label0_conductive, {"diffusivities": {0: 1.0, 1: 0.0}},
+                  {"iter_limit": 1000}, "test_taufactor.py:180-187"),
+    "mp_slanted": ("multiphase", _slanted, {}, {"iter_limit": 1000}, "test_taufactor.py:195-205"),
+    "mp_batched": ("multiphase", _batched_mp, {"diffusivities": {0: 0.0, 1: 1.0, 2: 0.5}},
+                   {"iter_limit": 1000}, "test_taufactor.py:207-224"),
+    "pmp_ones": ("periodic_multiphase", lambda: np.ones((20, 20, 20)), {"diffusivities": {1: 1.0}},
+                 {"iter_limit": 1000}, "test_taufactor.py:226-232"),
+    "pmp_slanted": ("periodic_multiphase", _slanted, {"diffusivities": {0: 0.0, 1: 1.0}},
+                    {"iter_limit": 1000}, "test_taufactor.py:234-247"),
+    "aniso_slanted": ("anisotropic", _slanted, {"spacing": (1.0, 1.5, 0.8)}, {}, "taufactor.py:422-478"),
+    "bernoulli100": ("binary", bernoulli_100, {}, {"conv_crit": 2e-2}, "100^3 Bernoulli(0.5), seed 0"),
+    "bernoulli100_periodic": ("periodic", bernoulli_100, {}, {"conv_crit": 2e-2},
+                              "100^3 Bernoulli(0.5), seed 0, periodic y/z"),
+}
+
+# name -> (kind, input builder, constructor kwargs, number of half-sweeps)
+SWEEP_CASES = {
+    "sw_binary": ("binary", lambda: random_binary((13, 10, 12), 11), {}, 57),
+    "sw_binary_batch": ("binary", lambda: random_binary((3, 9, 8, 11), 12), {}, 40),
+    "sw_periodic_even": ("periodic", lambda: random_binary((11, 10, 12), 13), {}, 57),
+    "sw_periodic_odd": ("periodic", lambda: random_binary((10, 9, 11), 14), {}, 57),
+    "sw_aniso": ("anisotropic", lambda: random_binary((12, 9, 10), 15), {"spacing": (1.0, 1.3, 0.7)}, 41),
+    "sw_multiphase": ("multiphase", lambda: random_labels((12, 10, 9), 16),
+                      {"diffusivities": {0: 0.0, 1: 1.0, 2: 0.1}}, 57),
+    "sw_periodic_multiphase": ("periodic_multiphase", lambda: random_labels((10, 9, 11), 17),
+                               {"diffusivities": {0: 0.3, 1: 1.0, 2: 0.1}}, 57),
+}

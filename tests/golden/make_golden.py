@@ -1,0 +1,87 @@
+"""Generate ``reference_outputs.npz`` by running the reference package itself.
+
+Usage (needs the reference source tree; see oracle/ref_shim.py):
+
+    python tests/golden/make_golden.py
+
+For every case in ``cases.SOLVE_CASES`` the reference solver class is built with
+``device='cpu'`` and ``solve(verbose=False, **solve_kwargs)`` is run; tau, D_eff, the iteration
+count, the convergence flag and the layer arrays (flux_1d, c_x, tau_x) are stored. For every
+case in ``cases.SWEEP_CASES`` the reference loop body (taufactor/taufactor.py:175-182) is run the
+given number of times and the padded float32 field is stored bit for bit.
+"""
+from __future__ import annotations
+
+import contextlib
+import io
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+sys.path.insert(0, HERE)
+
+from cases import SOLVE_CASES, SWEEP_CASES  # noqa: E402
+from oracle.ref_shim import import_reference  # noqa: E402
+
+CLASS_OF = {
+    "binary": "Solver",
+    "periodic": "PeriodicSolver",
+    "anisotropic": "AnisotropicSolver",
+    "multiphase": "MultiPhaseSolver",
+    "periodic_multiphase": "PeriodicMultiPhaseSolver",
+}
+
+
+def build(tau, kind, img, kw):
+    cls = getattr(tau, CLASS_OF[kind])
+    if kind in ("multiphase", "periodic_multiphase"):
+        ds = kw.get("diffusivities")
+        return cls(img, dict(ds) if ds is not None else None, device="cpu")
+    if kind == "anisotropic":
+        return cls(img, kw["spacing"], device="cpu")
+    return cls(img, device="cpu")
+
+
+def main():
+    import torch
+
+    tau = import_reference()
+    if tau is None:
+        raise SystemExit("reference source tree not found")
+    torch.manual_seed(0)
+    out = {}
+    for name, (kind, make, kw, solve_kw, _src) in SOLVE_CASES.items():
+        img = make()
+        with contextlib.redirect_stdout(io.StringIO()):
+            s = build(tau, kind, img, kw)
+            s.solve(verbose=False, **solve_kw)
+        out[f"{name}/tau"] = np.asarray(s.tau, dtype=np.float64)
+        out[f"{name}/D_eff"] = np.asarray(s.D_eff, dtype=np.float64)
+        out[f"{name}/iter"] = np.asarray(s.iter)
+        out[f"{name}/converged"] = np.asarray(bool(s.converged))
+        out[f"{name}/flux_1d"] = np.asarray(s.flux_1d, dtype=np.float64)
+        out[f"{name}/c_x"] = np.asarray(s.c_x, dtype=np.float64)
+        out[f"{name}/tau_x"] = np.asarray(s.tau_x, dtype=np.float64)
+        print(f"{name:24s} iter={s.iter:5d} tau={np.asarray(s.tau)} D_eff={np.asarray(s.D_eff)}")
+    for name, (kind, make, kw, n) in SWEEP_CASES.items():
+        img = make()
+        s = build(tau, kind, img, kw)
+        with torch.no_grad():
+            for _ in range(n):
+                s.apply_boundary_conditions()
+                inc = s.sum_weighted_neighbours()
+                inc /= s.factor
+                inc -= s.field[:, 1:-1, 1:-1, 1:-1]
+                inc *= s.cb[s.iter % 2]
+                s.field[:, 1:-1, 1:-1, 1:-1] += inc
+                s.iter += 1
+        out[f"{name}/field"] = s.field.numpy().copy()
+        print(f"{name:24s} field {tuple(s.field.shape)} after {n} half-sweeps")
+    np.savez_compressed(os.path.join(HERE, "reference_outputs.npz"), **out)
+
+
+if __name__ == "__main__":
+    main()

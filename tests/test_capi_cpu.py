@@ -1,0 +1,147 @@
+"""CPU tests of the C ABI and of the host-side logic (no kernel launches)."""
+import ctypes as C
+import re
+import warnings
+
+import numpy as np
+import pytest
+
+from taufactor_gb300 import _capi
+from taufactor_gb300.solvers import (AnisotropicSolver, MultiPhaseSolver, Solver, anisotropic_divisors,
+                                     harmonic_face)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    import os
+
+    if not os.path.exists(_capi.lib_path()):
+        from taufactor_gb300.build import build
+
+        build()
+    return _capi.load()
+
+
+def test_header_declares_exactly_the_exports(lib):
+    import os
+
+    hdr = open(os.path.join(os.path.dirname(os.path.dirname(__file__)), "include", "taufactor_gb300.h")).read()
+    declared = set(re.findall(r"\b(tf_[a-z_0-9]+)\s*\(", hdr))
+    assert declared == set(_capi.EXPORTS)
+    for name in declared:
+        assert hasattr(lib, name), name
+
+
+def test_version_and_status(lib):
+    assert b"sm_103a" in lib.tf_version()
+    assert lib.tf_status_string(0) == b"ok"
+    assert lib.tf_status_string(_capi.TF_ERR_TIMEOUT) == b"device wait timed out"
+
+
+def test_geometry(lib):
+    g = _capi.TfGeom()
+    assert lib.tf_geometry(2, 10, 9, 13, 0, C.byref(g)) == 0
+    assert (g.batch, g.nx, g.ny, g.nz) == (2, 10, 9, 13)
+    assert g.yp == 9 + 2 * g.halo_y
+    assert g.zh % 4 == 0 and g.zh >= 7 + 2 * g.halo_j
+    assert g.zhc % 16 == 0 and g.zhc >= g.zh
+    assert g.field_elems == 2 * 10 * g.yp * 2 * g.zh
+    assert g.code_bytes == 2 * 10 * g.yp * 2 * g.zhc
+    assert g.tiled == 1
+    assert lib.tf_geometry(1, 10, 9, 13, _capi.TF_PERIODIC_Y, C.byref(g)) == 0 and g.tiled == 0
+    assert lib.tf_geometry(1, 10, 10, 16, 3, C.byref(g)) == 0 and g.tiled == 1
+    assert lib.tf_geometry(0, 10, 9, 13, 0, C.byref(g)) == _capi.TF_ERR_ARG
+
+
+def test_entry_points_reject_bad_arguments_without_launching(lib):
+    g = _capi.TfGeom()
+    lib.tf_geometry(1, 8, 8, 8, 0, C.byref(g))
+    op = _capi.TfOperator()
+    op.omega = 1.5
+    n0 = lib.tf_launch_count()
+    assert lib.tf_pack(C.byref(g), C.byref(op), None, None, None, None, None) == _capi.TF_ERR_ARG
+    res = C.c_int(0)
+    assert lib.tf_advance(C.byref(g), C.byref(op), None, None, None, 0, 4, None, C.byref(res), None) == \
+        _capi.TF_ERR_ARG
+    bad = _capi.TfGeom.from_buffer_copy(g)
+    bad.zh = 3
+    assert lib.tf_layer_sums(C.byref(bad), C.byref(op), 16, 16, 16, 16, None) == _capi.TF_ERR_ARG
+    op.kind = 7
+    assert lib.tf_unpack(C.byref(g), C.byref(op), 16, 16, None) == _capi.TF_ERR_ARG
+    assert lib.tf_launch_count() == n0
+    with pytest.raises(ValueError):
+        _capi.check(_capi.TF_ERR_ARG, "x")
+    with pytest.raises(_capi.TfError):
+        _capi.check(_capi.TF_ERR_CUDA, "x")
+
+
+def test_anisotropic_divisors_match_reference_order():
+    """LUT entries equal the reference's rolled sums on a volume exercising every pattern."""
+    from oracle.sor import neighbour_counts
+
+    ky, kz = (1.0 / 1.3) ** 2, (1.0 / 0.7) ** 2
+    lut = anisotropic_divisors(ky, kz)
+    rng = np.random.default_rng(3)
+    mask = (rng.random((1, 7, 9, 11)) < 0.6).astype(np.float32)
+    nn = neighbour_counts(mask, False, (1.0, ky, kz))
+    p = np.pad(mask[0], 1)
+    p[0] = 2
+    p[-1] = 2
+    for x in range(7):
+        for y in range(9):
+            for z in range(11):
+                if mask[0, x, y, z] == 0:
+                    continue
+                xm, xp = int(p[x, y + 1, z + 1]), int(p[x + 2, y + 1, z + 1])
+                ym, yp = int(p[x + 1, y, z + 1]), int(p[x + 1, y + 2, z + 1])
+                zm, zp = int(p[x + 1, y + 1, z]), int(p[x + 1, y + 1, z + 2])
+                idx = 1 + xm + 3 * xp + 9 * ym + 18 * yp + 36 * zm + 72 * zp
+                assert lut[idx] == nn[0, x, y, z] or (np.isinf(lut[idx]) and np.isinf(nn[0, x, y, z]))
+
+
+def test_harmonic_face_matches_reference_formula():
+    from oracle.sor import harmonic_mean
+
+    vals = np.array([0.0, 0.1, 0.5, 1.0, 2.0, 0.3, 1e-3], dtype=np.float32)
+    a, b = np.meshgrid(vals, vals, indexing="ij")
+    hm = harmonic_mean(a, b)
+    for i in range(len(vals)):
+        for j in range(len(vals)):
+            assert harmonic_face(vals[i], vals[j]) == hm[i, j]
+
+
+def test_validation_errors_match_reference():
+    with pytest.raises(TypeError):
+        Solver([[0, 1], [1, 0]])
+    with pytest.raises(ValueError, match="Input image must only contain 0s and 1s"):
+        Solver(np.full((4, 4, 4), 2))
+    with pytest.raises(ValueError, match=r"expected \[B, X, Y, Z\]"):
+        Solver(np.ones((1, 1, 2, 2, 2)))
+    with pytest.raises(ValueError):
+        MultiPhaseSolver(np.zeros((6, 6, 6)), {0: 1.0, 1: -0.1})
+    with pytest.raises(TypeError):
+        MultiPhaseSolver(np.zeros((6, 6, 6)), [1, 2])
+    with pytest.raises(TypeError):
+        MultiPhaseSolver(np.zeros((6, 6, 6)), {"a": 1.0})
+    with pytest.raises(ValueError, match="spacing"):
+        AnisotropicSolver(np.ones((4, 4, 4)), (1, 2))
+
+
+def test_no_cpu_fallback():
+    """The reference falls back to the CPU; this build refuses."""
+    with pytest.raises(RuntimeError, match="CUDA"):
+        Solver(np.ones((4, 4, 4)), device="cpu")
+
+
+def test_multiphase_missing_label_warning_before_device():
+    img = np.zeros((6, 6, 6))
+    img[:, :, 3:] = 2
+    ds = {0: 1.0}
+    with warnings.catch_warnings(record=True) as w:
+        warnings.simplefilter("always")
+        try:
+            MultiPhaseSolver(img, ds, device="cpu")
+        except RuntimeError:
+            pass
+    assert any("assuming these phases are isolating." in str(x.message) for x in w)
+    assert ds[2] == 0.0

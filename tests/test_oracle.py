@@ -1,0 +1,90 @@
+"""CPU tests: the oracle against the reference's own outputs (tests/golden).
+
+The goldens were produced by running the reference package (tests/golden/make_golden.py).
+These tests pin the restatement before it is trusted as the checker of the CUDA path.
+"""
+import numpy as np
+import pytest
+
+from cases import SOLVE_CASES, SWEEP_CASES
+from oracle.fp64 import d_eff_fp64
+from oracle.percolation import spans_axis0
+from oracle.sor import OracleSolve
+
+SMALL_SOLVES = [k for k in SOLVE_CASES if not k.startswith("bernoulli")]
+
+
+@pytest.mark.parametrize("name", list(SWEEP_CASES))
+def test_oracle_half_sweeps_bitwise(name, golden):
+    kind, make, kw, n = SWEEP_CASES[name]
+    o = OracleSolve(make(), kind=kind, **kw)
+    o.half_sweep(n)
+    ref = golden[f"{name}/field"]
+    # bitwise up to the sign of zero (x == y compares -0.0 equal to 0.0)
+    assert np.array_equal(o.field, ref)
+
+
+@pytest.mark.parametrize("name", SMALL_SOLVES + ["bernoulli100"])
+def test_oracle_solve_matches_reference(name, golden):
+    kind, make, kw, solve_kw, _ = SOLVE_CASES[name]
+    o = OracleSolve(make(), kind=kind, **kw)
+    o.solve(**solve_kw)
+    assert o.iter == int(golden[f"{name}/iter"])
+    assert bool(o.converged) == bool(golden[f"{name}/converged"])
+    tau_ref = golden[f"{name}/tau"]
+    d_ref = golden[f"{name}/D_eff"]
+    assert np.array_equal(np.isinf(o.tau), np.isinf(tau_ref))
+    fin = np.isfinite(tau_ref)
+    # the oracle reduces layer means in float64, the reference in float32
+    np.testing.assert_allclose(o.tau[fin], tau_ref[fin], rtol=2e-6)
+    np.testing.assert_allclose(o.D_eff, d_ref, rtol=2e-6, atol=1e-9)
+    np.testing.assert_allclose(o.flux_1d, golden[f"{name}/flux_1d"], rtol=1e-4, atol=1e-7)
+
+
+def test_reference_known_answers_through_oracle(golden):
+    """The reference test-suite's own pins (tests/test_taufactor.py) hold for the oracle."""
+    o = OracleSolve(SOLVE_CASES["slanted"][1](), kind="binary")
+    o.solve()
+    assert np.around(o.tau, decimals=5) == 7.51667
+    for name in ("blocks_cube", "blocks_long_x", "blocks_long_z", "strip", "p_blocks", "p_strip"):
+        kind, make, kw, skw, _ = SOLVE_CASES[name]
+        o = OracleSolve(make(), kind=kind, **kw)
+        o.solve(**skw)
+        assert np.around(o.tau, decimals=5) == 1.0
+    for name in ("nonperc", "deadend", "p_nonperc", "mp_nonperc"):
+        kind, make, kw, skw, _ = SOLVE_CASES[name]
+        o = OracleSolve(make(), kind=kind, **kw)
+        o.solve(**skw)
+        assert np.all(o.tau == np.inf)
+        assert np.around(o.D_eff, 5) == 0
+
+
+@pytest.mark.parametrize("name", ["slanted", "strip", "mp_strip12", "mp_strip123", "pmp_slanted", "aniso_slanted",
+                                  "blocks_long_x"])
+def test_fp64_oracle_matches_reference_known_answers(name, golden):
+    kind, make, kw, _, _ = SOLVE_CASES[name]
+    o = OracleSolve(make(), kind=kind, **kw)
+    d, _, resid = d_eff_fp64(o)
+    assert np.all(resid < 1e-9)
+    np.testing.assert_allclose(d, golden[f"{name}/D_eff"], rtol=2e-6)
+
+
+def test_fp64_oracle_bernoulli100(golden):
+    """The reference at conv_crit 2e-2 sits ~1e-4 from the FP64 solution of its own operator."""
+    o = OracleSolve(SOLVE_CASES["bernoulli100"][1](), kind="binary")
+    d, _, resid = d_eff_fp64(o)
+    assert resid[0] < 1e-9
+    ref = golden["bernoulli100/D_eff"][0]
+    assert abs(d[0] - ref) / d[0] < 3e-4
+    np.testing.assert_allclose(d[0], 0.10480938, rtol=1e-6)
+
+
+def test_percolation_restatement():
+    m = np.zeros((6, 5, 5), dtype=bool)
+    assert not spans_axis0(m)
+    m[:, 2, 2] = True
+    assert spans_axis0(m)
+    m[3, 2, 2] = False
+    assert not spans_axis0(m)
+    m[2:5, 2, 3] = True  # detour around the gap
+    assert spans_axis0(m)
