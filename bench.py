@@ -282,6 +282,25 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def run_profile(args):
+    """Small fixed workload for profiler captures: `--half-sweeps` half-sweeps of a
+    `--batch` x `--side`^3 batch after 8 warm-up half-sweeps. Prints nothing to measure."""
+    import torch
+
+    import taufactor_gb300 as tg
+    from taufactor_gb300.synthetic import batch_256
+
+    vols = batch_256(args.batch, args.side, SIGMA)
+    cls = tg.PeriodicSolver if args.periodic else tg.Solver
+    s = cls(vols, device="cuda")
+    s._advance(8)
+    torch.cuda.synchronize()
+    s._advance(args.half_sweeps)
+    s._layer_means()
+    torch.cuda.synchronize()
+    print(f"profile workload done: {args.batch}x{args.side}^3, {args.half_sweeps} half-sweeps")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -289,8 +308,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", action="store_true", help="run the small profiler workload only")
+    ap.add_argument("--batch", type=int, default=4, help="--profile: volumes")
+    ap.add_argument("--side", type=int, default=256, help="--profile: volume side")
+    ap.add_argument("--half-sweeps", type=int, default=40, help="--profile: half-sweeps")
+    ap.add_argument("--periodic", action="store_true", help="--profile: PeriodicSolver")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.profile:
+        run_profile(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -67,6 +67,8 @@ typedef struct tf_operator {
     float ghost_lo, ghost_hi;  /* Dirichlet ghost values 2*bc: -1 (x = -1) and +1 (x = nx)     */
     float ky, kz;              /* anisotropic y, z weights (dx/dy)^2, (dx/dz)^2                */
     int32_t n_phases;          /* multiphase: phases 1..n_phases                               */
+    int32_t tile;              /* tiled-kernel tile shape: 0 = 16x64, 1 = 16x128, 2 = 32x64    */
+    int32_t k_max;             /* half-sweeps per tiled launch, 1..4 (0 = 4)                   */
     float divisor[256];        /* binary/anisotropic: code -> diagonal (inf = frozen voxel)    */
     float face[32 * 32];       /* multiphase: [phase a][phase b] harmonic face conductance     */
     uint8_t conductive[32];    /* multiphase: phase -> D > 0 (mask of the initial field)       */
@@ -128,6 +130,13 @@ int tf_unpack(const tf_geom* g, const tf_operator* op, const float* field_dev, f
  * (ghost cells are rebuilt). Used to resume from a user-supplied field. */
 int tf_repack(const tf_geom* g, const tf_operator* op, const float* padded_dev, float* field_dev,
               void* stream);
+
+/* Self-check of the binary sweep's division: for divisor n in 1..8, count the float32 inputs s
+ * (all finite bit patterns) where the kernel's exact division by n (one multiply and two FMAs
+ * with RN(1/n)) differs bitwise from IEEE division s / n. Adds the count to *bad_dev (uint64).
+ * No reference counterpart: it guards the bitwise parity of the update `sum / nn`
+ * (taufactor.py:177). */
+int tf_check_small_division(int n, uint64_t* bad_dev, void* stream);
 
 #ifdef __cplusplus
 }

@@ -19,7 +19,7 @@ TF_MAX_HALF_SWEEPS = 4
 # every symbol the header declares (checked by the CPU tests)
 EXPORTS = (
     "tf_version", "tf_status_string", "tf_launch_count", "tf_geometry", "tf_pack", "tf_advance",
-    "tf_layer_sums", "tf_unpack", "tf_repack",
+    "tf_layer_sums", "tf_unpack", "tf_repack", "tf_check_small_division",
 )
 
 
@@ -33,7 +33,8 @@ class TfGeom(C.Structure):
 class TfOperator(C.Structure):
     _fields_ = [("kind", C.c_int32), ("periodic", C.c_int32), ("omega", C.c_float),
                 ("ghost_lo", C.c_float), ("ghost_hi", C.c_float), ("ky", C.c_float), ("kz", C.c_float),
-                ("n_phases", C.c_int32), ("divisor", C.c_float * 256), ("face", C.c_float * 1024),
+                ("n_phases", C.c_int32), ("tile", C.c_int32), ("k_max", C.c_int32),
+                ("divisor", C.c_float * 256), ("face", C.c_float * 1024),
                 ("conductive", C.c_uint8 * 32)]
 
 
@@ -73,6 +74,7 @@ def load():
         "tf_layer_sums": (i32, [G, O, vp, vp, vp, vp, vp]),
         "tf_unpack": (i32, [G, O, vp, vp, vp]),
         "tf_repack": (i32, [G, O, vp, vp, vp]),
+        "tf_check_small_division": (i32, [i32, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

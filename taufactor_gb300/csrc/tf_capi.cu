@@ -134,8 +134,9 @@ int tf_advance(const tf_geom* g, const tf_operator* op, float* field_a_dev, floa
     float* out = field_b_dev;
     int in_b = 0;
     int left = n_half;
+    const int kmax = (op->k_max >= 1 && op->k_max <= HY) ? op->k_max : HY;
     while (left > 0) {
-        const int nh = left < HY ? left : HY;
+        const int nh = left < kmax ? left : kmax;
         const int rc = sweep_tiled(*g, *op, in, out, code_dev, colour, nh, err_dev, st);
         if (rc) return rc;
         colour ^= (nh & 1);
@@ -162,6 +163,11 @@ int tf_unpack(const tf_geom* g, const tf_operator* op, const float* field_dev, f
 int tf_repack(const tf_geom* g, const tf_operator* op, const float* padded_dev, float* field_dev, void* stream) {
     if (!valid_geom(g) || !valid_op(op) || !field_dev || !padded_dev) return TF_ERR_ARG;
     return repack(*g, *op, padded_dev, field_dev, (cudaStream_t)stream);
+}
+
+int tf_check_small_division(int n, uint64_t* bad_dev, void* stream) {
+    if (n < 1 || n > 8 || !bad_dev) return TF_ERR_ARG;
+    return check_small_division(n, reinterpret_cast<unsigned long long*>(bad_dev), (cudaStream_t)stream);
 }
 
 }  // extern "C"

@@ -101,11 +101,38 @@ __device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, u
 // The reference evaluates (taufactor.py:176-181), per voxel and in float32 with one rounding
 // per operation: inc = sum / div; inc -= c; inc *= omega; c += inc. The _rn intrinsics keep
 // the compiler from contracting the multiply-add into an FMA.
-__device__ __forceinline__ float sor_update(float c, float sum, float div, float omega) {
-    float inc = __fdiv_rn(sum, div);
-    inc = __fsub_rn(inc, c);
+__device__ __forceinline__ float sor_finish(float c, float quot, float omega) {
+    float inc = __fsub_rn(quot, c);
     inc = __fmul_rn(inc, omega);
     return __fadd_rn(c, inc);
+}
+
+// sum / div for an arbitrary positive divisor, inf allowed. A finite sum over an infinite
+// divisor is a signed zero, and 0 / div is a signed zero; both are returned without dividing,
+// which keeps the division on its fast path.
+__device__ __forceinline__ float quotient(float sum, float div) {
+    if (div == __int_as_float(0x7f800000) || sum == 0.0f) return __fmul_rn(sum, 0.0f);
+    return __fdiv_rn(sum, div);
+}
+
+// Correctly rounded sum / n for n in 1..8 given r = RN(1/n): one multiply and two fused
+// multiply-adds (Brisebarre, Muller, Raina, "Accelerating correctly rounded floating-point
+// division when the divisor is known in advance", IEEE Trans. Computers 53(8), 2004):
+// q = RN(s*r); e = s - q*n (exact by FMA); result = RN(q + e*r), or q itself when e is 0
+// (q is then exact, and returning it keeps the sign of a zero quotient). For these divisors the
+// result equals IEEE division for finite float32 s with |s| >= 2^-90 (below that the product
+// e*r may underflow); div_small_exact() adds IEEE division for the tiny range.
+// tf_check_small_division() verifies div_small_exact exhaustively against the hardware division
+// on the GPU. (Infinite s never occurs: the dividend is a sum of finite field values.)
+__device__ __forceinline__ float div_small(float s, float n, float r) {
+    const float q = __fmul_rn(s, r);
+    const float e = __fmaf_rn(-q, n, s);
+    return e == 0.0f ? q : __fmaf_rn(e, r, q);
+}
+
+// div_small with the tiny-dividend fallback used by the sweeps: exact for every finite s.
+__device__ __forceinline__ float div_small_exact(float s, float n, float r) {
+    return (s != 0.0f && fabsf(s) < 0x1p-90f) ? __fdiv_rn(s, n) : div_small(s, n, r);
 }
 
 }  // namespace tf

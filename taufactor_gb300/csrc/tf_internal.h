@@ -9,21 +9,19 @@
 
 namespace tf {
 
-constexpr int TILE_Y = 16;  // tile rows (y) of the tiled sweep
-constexpr int TILE_Z = 64;  // tile columns (z) of the tiled sweep (multiple of 32)
-
 void note_launch();
 
 // 3-D tiled tensor map over [dim2][dim1][dim0] with the given byte strides of dims 1 and 2.
 int encode_map_3d(CUtensorMap* map, const void* base, int elem_bytes, long long dim0, long long dim1,
                   long long dim2, long long stride1_bytes, long long stride2_bytes, int box0, int box1);
 
+// K = n_half (1..TF_MAX_HALF_SWEEPS) half-sweeps in one register-streaming launch, in -> out.
 int sweep_tiled(const tf_geom& g, const tf_operator& op, const float* in, float* out, const uint8_t* code,
                 int first_colour, int n_half, int32_t* err, cudaStream_t st);
 int sweep_plain(const tf_geom& g, const tf_operator& op, float* f, const uint8_t* code, int colour,
                 cudaStream_t st);
 int refresh_ghosts(const tf_geom& g, int periodic, float* f, cudaStream_t st);
-int tiled_smem_bytes();
+int check_small_division(int n, unsigned long long* bad_dev, cudaStream_t st);
 
 int pack(const tf_geom& g, const tf_operator& op, const uint8_t* phase, const float* profile, uint8_t* code,
          float* field, cudaStream_t st);

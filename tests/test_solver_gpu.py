@@ -164,3 +164,31 @@ def test_bad_arguments_raise():
     rc = s._lib.tf_advance(None, None, None, None, None, 0, 1, None, None, None)
     with pytest.raises(ValueError):
         check(rc, "tf_advance")
+
+
+def test_small_integer_division_is_ieee():
+    """The binary update divides by nn with one multiply and two FMAs; check every finite input."""
+    from taufactor_gb300 import _capi
+
+    lib = _capi.load()
+    bad = torch.zeros(9, dtype=torch.int64, device="cuda")
+    for n in range(1, 9):
+        _capi.check(lib.tf_check_small_division(n, bad[n:].data_ptr(), torch.cuda.current_stream().cuda_stream),
+                    "tf_check_small_division")
+    assert bad.cpu().tolist() == [0] * 9
+
+
+@pytest.mark.parametrize("k_max", [2, 3, 4])
+@pytest.mark.parametrize("tile", [0, 1, 2])
+@pytest.mark.parametrize("kind", ["binary", "periodic"])
+def test_tile_variants_bitwise(kind, tile, k_max):
+    """Every tile shape and fused depth of the kernel gives the reference iterations bit for bit."""
+    img = random_binary((2, 21, 52, 136), 31 + tile)
+    o = OracleSolve(img, kind=kind)
+    s = make_solver(kind, img, {})
+    s._op.tile = tile
+    s._op.k_max = k_max
+    for n in (4, 4, 3, 8, 1, 12):
+        s._advance(n)
+        o.half_sweep(n)
+        assert np.array_equal(interior_and_x_ghosts(s.field.cpu().numpy()), interior_and_x_ghosts(o.field)), n
