@@ -112,6 +112,36 @@ int tf_advance(const tf_geom* g, const tf_operator* op, float* field_a_dev, floa
                const uint8_t* code_dev, int first_colour, int n_half, int32_t* err_dev,
                int* result_in_b, void* stream);
 
+/* tf_advance for a correction solve A e = r: every update adds rhs_dev (float [field_elems],
+ * split layout with periodic ghost copies, as written by tf_residual_f64) to the neighbour sum.
+ * Use an operator whose ghost_lo/ghost_hi are 0 (homogeneous Dirichlet faces). No reference
+ * counterpart: the reference iterates in float32 only (taufactor.py:172-182). */
+int tf_advance_rhs(const tf_geom* g, const tf_operator* op, float* field_a_dev, float* field_b_dev,
+                   const uint8_t* code_dev, const float* rhs_dev, int first_colour, int n_half,
+                   int32_t* err_dev, int* result_in_b, void* stream);
+
+/* float32 field -> float64 field (same split layout, double [field_elems]). */
+int tf_widen_f64(const tf_geom* g, const float* field_dev, double* field64_dev, void* stream);
+
+/* float64 field -> float32 field; periodic ghost cells are rebuilt. */
+int tf_narrow_f64(const tf_geom* g, const tf_operator* op, const double* field64_dev, float* field_dev,
+                  void* stream);
+
+/* field64 += e (float32), every element. */
+int tf_axpy_f64(const tf_geom* g, double* field64_dev, const float* e_dev, void* stream);
+
+/* float64 residual r = b - A c of the operator the reference's iteration converges to
+ * (A c = d c - weighted in-volume neighbour sum, b = Dirichlet ghost terms; taufactor.py:95-103,
+ * :176-181, :598-613). Writes r as float32 into rhs_dev (split layout, periodic ghost copies)
+ * and per-plane float64 sums of r^2 and b^2 into r2_sum_dev / b2_sum_dev [batch][nx]. */
+int tf_residual_f64(const tf_geom* g, const tf_operator* op, const double* field64_dev,
+                    const uint8_t* code_dev, float* rhs_dev, double* r2_sum_dev, double* b2_sum_dev,
+                    void* stream);
+
+/* tf_layer_sums on a float64 field (differences and products in float64). */
+int tf_layer_sums_f64(const tf_geom* g, const tf_operator* op, const double* field64_dev,
+                      const uint8_t* code_dev, double* flux_sum_dev, double* c_sum_dev, void* stream);
+
 /* Per-layer float64 sums (not means) for the convergence metrics. Replaces
  * Solver.vertical_flux / MultiPhaseSolver.vertical_flux (taufactor.py:412-419, :615-620) with
  * torch.mean(..., (2, 3)) (:296) and the c_x mean (:307).

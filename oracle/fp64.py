@@ -11,7 +11,11 @@ converges to (tldr-group/taufactor v1.2.1, taufactor/taufactor.py):
   :626-656);
 * Dirichlet inlet/outlet: a voxel on x = 0 (x = Nx-1) couples to the boundary value -0.5
   (+0.5) with twice its boundary-face conductance, because the boundary sits half a voxel away
-  (the 2 in the padding of :404 and the extra D_x term of :601-602).
+  (the 2 in the padding of :404 and the extra D_x term of :601-602);
+* coefficients exactly as the reference iteration uses them: float32 face values (the float32
+  (dx/dy)^2 weights of the anisotropic solver) and, as the diagonal, the reference's float32
+  divisor ``factor`` (nn or the float32 sum of faces), so the FP64 solution is the fixed point of
+  the reference's own discrete operator.
 
 Voxels of clusters that touch neither Dirichlet face make the operator singular; they carry no
 flux at convergence, so they are removed (pinned to 0). The system is solved with
@@ -50,8 +54,8 @@ def _face_weights(o: OracleSolve):
         gb_hi = o.D_x[:, -1].astype(np.float64)
         return gx, gy, gz, gb_lo, gb_hi
     m = o.mask.astype(np.float64)
-    ky = getattr(o, "Ky", 1.0)
-    kz = getattr(o, "Kz", 1.0)
+    ky = float(np.float32(getattr(o, "Ky", 1.0)))
+    kz = float(np.float32(getattr(o, "Kz", 1.0)))
     gx = np.zeros_like(m)
     gx[:, :-1] = m[:, :-1] * m[:, 1:]
     if o.periodic:
@@ -101,6 +105,9 @@ def assemble(o: OracleSolve, b: int):
     anchored = np.zeros(ncomp, dtype=bool)
     anchored[comp[dirichlet]] = True
     keep = active & anchored[comp]
+    # the reference's float32 divisor (finite where the voxel is updated)
+    fac = o.factor[b].astype(np.float64).ravel()
+    diag = np.where(np.isfinite(fac) & (diag > 0), fac, diag)
     A = (off + sp.diags(diag)).tocsr()
     k = np.nonzero(keep)[0]
     return A[k][:, k].tocsr(), rhs[k], k
@@ -134,8 +141,10 @@ def layer_flux_fp64(o: OracleSolve, field: np.ndarray) -> np.ndarray:
     d = field[:, 1:] - field[:, :-1]
     if o.multiphase:
         return (o.D_x[:, 1:-1].astype(np.float64) * d).mean(axis=(2, 3))
-    fin = np.isfinite(o.factor)
-    d = d * (fin[:, :-1] & fin[:, 1:])
+    # Solver.vertical_flux zeroes faces whose divisor exceeds 8 (:417-418; for the anisotropic
+    # solver this also drops finite divisors above 8)
+    ok = o.factor <= 8
+    d = d * (ok[:, :-1] & ok[:, 1:])
     return d.mean(axis=(2, 3))
 
 

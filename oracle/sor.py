@@ -253,11 +253,18 @@ class OracleSolve:
         return (f[:, 2:, 1:-1, 1:-1] + f[:, :-2, 1:-1, 1:-1] + f[:, 1:-1, 2:, 1:-1]
                 + f[:, 1:-1, :-2, 1:-1] + f[:, 1:-1, 1:-1, 2:] + f[:, 1:-1, 1:-1, :-2])
 
-    def half_sweep(self, n: int = 1):
-        """n reference iterations (each one colour): taufactor.py:174-182."""
+    def half_sweep(self, n: int = 1, rhs=None):
+        """n reference iterations (each one colour): taufactor.py:174-182.
+
+        ``rhs`` (float32 [B,X,Y,Z], no reference counterpart) is added to the neighbour sum, which
+        turns the iteration into SOR for A e = rhs; it restates the correction solve of the
+        FP64 defect correction.
+        """
         for _ in range(n):
             self.apply_boundary_conditions()
             inc = self.neighbour_sum()
+            if rhs is not None:
+                inc += rhs
             inc /= self.factor
             inc -= self.field[:, 1:-1, 1:-1, 1:-1]
             inc *= self.cb[self.iter % 2]

@@ -19,7 +19,8 @@ TF_MAX_HALF_SWEEPS = 4
 # every symbol the header declares (checked by the CPU tests)
 EXPORTS = (
     "tf_version", "tf_status_string", "tf_launch_count", "tf_geometry", "tf_pack", "tf_advance",
-    "tf_layer_sums", "tf_unpack", "tf_repack", "tf_check_small_division",
+    "tf_layer_sums", "tf_unpack", "tf_repack", "tf_check_small_division", "tf_advance_rhs", "tf_widen_f64",
+    "tf_narrow_f64", "tf_axpy_f64", "tf_residual_f64", "tf_layer_sums_f64",
 )
 
 
@@ -75,6 +76,12 @@ def load():
         "tf_unpack": (i32, [G, O, vp, vp, vp]),
         "tf_repack": (i32, [G, O, vp, vp, vp]),
         "tf_check_small_division": (i32, [i32, vp, vp]),
+        "tf_advance_rhs": (i32, [G, O, vp, vp, vp, vp, i32, i32, vp, C.POINTER(C.c_int), vp]),
+        "tf_widen_f64": (i32, [G, vp, vp, vp]),
+        "tf_narrow_f64": (i32, [G, O, vp, vp, vp]),
+        "tf_axpy_f64": (i32, [G, vp, vp, vp]),
+        "tf_residual_f64": (i32, [G, O, vp, vp, vp, vp, vp, vp]),
+        "tf_layer_sums_f64": (i32, [G, O, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -110,9 +110,9 @@ int tf_pack(const tf_geom* g, const tf_operator* op, const uint8_t* phase_dev, c
     return pack(*g, *op, phase_dev, profile_dev, code_dev, field_dev, (cudaStream_t)stream);
 }
 
-int tf_advance(const tf_geom* g, const tf_operator* op, float* field_a_dev, float* field_b_dev,
-               const uint8_t* code_dev, int first_colour, int n_half, int32_t* err_dev, int* result_in_b,
-               void* stream) {
+static int advance_impl(const tf_geom* g, const tf_operator* op, float* field_a_dev, float* field_b_dev,
+                        const uint8_t* code_dev, const float* rhs_dev, int first_colour, int n_half, int32_t* err_dev,
+                        int* result_in_b, void* stream) {
     if (!valid_geom(g) || !valid_op(op) || !field_a_dev || !field_b_dev || !code_dev || !result_in_b || n_half < 0 ||
         field_a_dev == field_b_dev)
         return TF_ERR_ARG;
@@ -124,7 +124,7 @@ int tf_advance(const tf_geom* g, const tf_operator* op, float* field_a_dev, floa
     int colour = first_colour & 1;
     if (!tiled) {
         for (int i = 0; i < n_half; ++i, colour ^= 1) {
-            const int rc = sweep_plain(*g, *op, field_a_dev, code_dev, colour, st);
+            const int rc = sweep_plain(*g, *op, field_a_dev, code_dev, rhs_dev, colour, st);
             if (rc) return rc;
         }
         *result_in_b = 0;
@@ -137,7 +137,7 @@ int tf_advance(const tf_geom* g, const tf_operator* op, float* field_a_dev, floa
     const int kmax = (op->k_max >= 1 && op->k_max <= HY) ? op->k_max : HY;
     while (left > 0) {
         const int nh = left < kmax ? left : kmax;
-        const int rc = sweep_tiled(*g, *op, in, out, code_dev, colour, nh, err_dev, st);
+        const int rc = sweep_tiled(*g, *op, in, out, code_dev, rhs_dev, colour, nh, err_dev, st);
         if (rc) return rc;
         colour ^= (nh & 1);
         left -= nh;
@@ -146,6 +146,51 @@ int tf_advance(const tf_geom* g, const tf_operator* op, float* field_a_dev, floa
     }
     *result_in_b = in_b;
     return TF_OK;
+}
+
+int tf_advance(const tf_geom* g, const tf_operator* op, float* field_a_dev, float* field_b_dev,
+               const uint8_t* code_dev, int first_colour, int n_half, int32_t* err_dev, int* result_in_b,
+               void* stream) {
+    return advance_impl(g, op, field_a_dev, field_b_dev, code_dev, nullptr, first_colour, n_half, err_dev,
+                        result_in_b, stream);
+}
+
+int tf_advance_rhs(const tf_geom* g, const tf_operator* op, float* field_a_dev, float* field_b_dev,
+                   const uint8_t* code_dev, const float* rhs_dev, int first_colour, int n_half, int32_t* err_dev,
+                   int* result_in_b, void* stream) {
+    if (!rhs_dev || (reinterpret_cast<uintptr_t>(rhs_dev) & 15)) return TF_ERR_ARG;
+    return advance_impl(g, op, field_a_dev, field_b_dev, code_dev, rhs_dev, first_colour, n_half, err_dev,
+                        result_in_b, stream);
+}
+
+int tf_widen_f64(const tf_geom* g, const float* field_dev, double* field64_dev, void* stream) {
+    if (!valid_geom(g) || !field_dev || !field64_dev) return TF_ERR_ARG;
+    return widen(*g, field_dev, field64_dev, (cudaStream_t)stream);
+}
+
+int tf_narrow_f64(const tf_geom* g, const tf_operator* op, const double* field64_dev, float* field_dev,
+                  void* stream) {
+    if (!valid_geom(g) || !valid_op(op) || !field_dev || !field64_dev) return TF_ERR_ARG;
+    return narrow(*g, *op, field64_dev, field_dev, (cudaStream_t)stream);
+}
+
+int tf_axpy_f64(const tf_geom* g, double* field64_dev, const float* e_dev, void* stream) {
+    if (!valid_geom(g) || !field64_dev || !e_dev) return TF_ERR_ARG;
+    return axpy(*g, field64_dev, e_dev, (cudaStream_t)stream);
+}
+
+int tf_residual_f64(const tf_geom* g, const tf_operator* op, const double* field64_dev, const uint8_t* code_dev,
+                    float* rhs_dev, double* r2_sum_dev, double* b2_sum_dev, void* stream) {
+    if (!valid_geom(g) || !valid_op(op) || !field64_dev || !code_dev || !rhs_dev || !r2_sum_dev || !b2_sum_dev)
+        return TF_ERR_ARG;
+    return residual(*g, *op, field64_dev, code_dev, rhs_dev, r2_sum_dev, b2_sum_dev, (cudaStream_t)stream);
+}
+
+int tf_layer_sums_f64(const tf_geom* g, const tf_operator* op, const double* field64_dev, const uint8_t* code_dev,
+                      double* flux_sum_dev, double* c_sum_dev, void* stream) {
+    if (!valid_geom(g) || !valid_op(op) || !field64_dev || !code_dev || !c_sum_dev || (g->nx > 1 && !flux_sum_dev))
+        return TF_ERR_ARG;
+    return layer_sums_f64(*g, *op, field64_dev, code_dev, flux_sum_dev, c_sum_dev, (cudaStream_t)stream);
 }
 
 int tf_layer_sums(const tf_geom* g, const tf_operator* op, const float* field_dev, const uint8_t* code_dev,

@@ -1,334 +1,21 @@
-// Register-streaming red-black SOR wavefront: K half-sweeps per launch (sm_103a).
-//
-// Each CTA owns a TY x TZ tile of the (y, z) plane (plus K ghost rows and one ghost float4
-// group on each side of every half-row) and marches along x. Planes are staged into a
-// shared-memory ring by TMA (cp.async.bulk.tensor + mbarrier, D planes ahead).
-//
-// One thread per (tile row, float4 group). A thread keeps its own 2 x 4 cells (even-z and odd-z
-// half-row groups) of the K+2 planes in flight in registers, indexed by *relative colour*
-// (colour XOR the launch's first colour), so half-sweep s of the launch always updates the
-// relative-colour (s-1)&1 registers: every register index is a compile-time constant after
-// unrolling. Half-sweep s is applied to plane t-s at step t (wavefront in x). x- and z-
-// neighbours come from the thread's registers; y-neighbours and the z-edge cell of the
-// adjacent group come from the plane's shared-memory slot, where every update is published.
-// Within a step no half-sweep reads shared memory written in the same step, so one CTA barrier
-// per plane suffices. The region updated by half-sweep s shrinks by one row per half-sweep, so
-// the tile interior is exact; it is written from registers to the other ping-pong buffer (plus
-// periodic ghost copies). The result is K reference iterations of taufactor.py:174-182,
-// bit for bit.
-#include "tf_common.cuh"
+// Dispatch of the register-streaming sweep to its per-operator translation units.
 #include "tf_internal.h"
-#include "tf_update.cuh"
 
 namespace tf {
 
-template <int TY, int TZ, int K>
-struct StreamShape {
-    static constexpr int TJ = TZ / 2;                // interior cells per half-row
-    static constexpr int G = TJ / 4 + 2;             // float4 groups per staged half-row
-    static constexpr int WJ = 4 * G;                 // floats per staged half-row
-    static constexpr int WJC = (WJ + 15) / 16 * 16;  // bytes per staged code half-row
-    static constexpr int ROWS = TY + 2 * K;          // staged rows: K ghost rows per side
-    static constexpr int NT = ROWS * G;              // one thread per (row, group)
-    static constexpr int R = K + 2;                  // planes held in registers
-    static constexpr int D = 3;                      // planes loaded ahead
-    static constexpr int NS = K + 1 + D;             // shared-memory slots
-    static constexpr int FBYTES = 2 * ROWS * WJ * 4;
-    static constexpr int CBYTES = 2 * ROWS * WJC;
-    static constexpr int GUARD = 128;                // readable guard around each field slot
-    static constexpr int FSPAN = (GUARD + FBYTES + GUARD + 127) / 128 * 128;
-    static constexpr int SLOT = FSPAN + (CBYTES + 127) / 128 * 128;
-    static constexpr int LUT_BYTES = 32 * 32 * 4;
-    static constexpr int HEAD = 128 + LUT_BYTES + 128;  // mbarriers, LUT, division table
-    static constexpr int SMEM = HEAD + NS * SLOT;
-    static_assert(TJ % 16 == 0, "tile z-extent must keep TMA box starts 16-byte aligned for codes");
-    static_assert(K >= 1 && K <= HY, "half-sweeps per launch exceed the ghost rows");
-};
-
-// Periodic ghost copies of one written float4 group for faces whose half-row length is not a
-// multiple of 4 (the common case is handled inline with float4 stores). Out of line.
-static __device__ __noinline__ void ghost_copies_scalar(float* outp, long long row_f, int zh, int ny, int nz, int y,
-                                                        int q, int j, int nj, float4 v, bool py) {
-    const int hz = nz >> 1;
-    const int ys = py && y < HY ? y + ny : (py && y >= ny - HY ? y - ny : y);
-    for (int pass = 0; pass < (ys != y ? 2 : 1); ++pass) {
-        const int yy = pass ? ys : y;
-        float* rowp = outp + (long long)(yy + HY) * row_f + q * zh + HJ;
-        for (int c = 0; c < 4 && j + c < nj; ++c) {
-            const int jc = j + c;
-            const float val = comp(v, c);
-            if (pass) rowp[jc] = val;
-            if (jc < HJ) rowp[jc + hz] = val;
-            else if (jc >= hz - HJ) rowp[jc - hz] = val;
-        }
-    }
-}
-
-// One half-sweep on the thread's float4 group at plane p (relative colour held in `self`).
-//   xp/xm: x-neighbour groups (registers; Dirichlet ghost planes are part of the ring);
-//   zo: the other half-row group of this plane (registers); y-neighbours and the z-edge cell of
-//   the adjacent group are read from the plane's shared-memory slot, and the result is
-//   published there.
-template <int KIND>
-__device__ __forceinline__ void stage_update(float4& self, const float4& xp, const float4& xm, const float4& zo,
-                                             uint32_t cc, uint32_t cxp, uint32_t cxm, uint32_t czo, float* Fp,
-                                             const unsigned char* Cp, int row_up, int row_dn, int row_me, int row_ot,
-                                             int jj, int q, int WJ, int WJC, bool at_lo, bool at_hi,
-                                             const SweepArgs& a, const float* lut, const float2* tab) {
-    const float4 yp = ld4(Fp + row_up * WJ + jj);
-    const float4 ym = ld4(Fp + row_dn * WJ + jj);
-    const int ej = q ? jj + 4 : jj - 1;
-    const float e = Fp[row_ot * WJ + ej];
-    float4 zp, zm;
-    z_neighbours(q, zo, e, zp, zm);
-    uint32_t cyp = 0, cym = 0, czp = 0, czm = 0;
-    if (KIND == TF_KIND_MULTIPHASE) {
-        cyp = ld_u32(Cp + row_up * WJC + jj);
-        cym = ld_u32(Cp + row_dn * WJC + jj);
-        const uint32_t ce = (ej >= 0 && ej < WJC) ? Cp[row_ot * WJC + ej] : 0u;
-        z_codes(q, czo, ce, czp, czm);
-    }
-    self = update4<KIND>(self, xp, xm, yp, ym, zp, zm, cc, cxp, cxm, cyp, cym, czp, czm, at_lo, at_hi, a.omega, a.ky,
-                         a.kz, lut, tab);
-    st4(Fp + row_me * WJ + jj, self);
-}
-
-template <int KIND, int TY, int TZ, int K>
-__global__ void __launch_bounds__(StreamShape<TY, TZ, K>::NT, StreamShape<TY, TZ, K>::NT <= 256 ? 2 : 1)
-    k_stream(const __grid_constant__ CUtensorMap tmf, const __grid_constant__ CUtensorMap tmc, const SweepArgs a,
-             const __grid_constant__ tf_operator op) {
-    using S = StreamShape<TY, TZ, K>;
-    constexpr int G = S::G, WJ = S::WJ, WJC = S::WJC, NS = S::NS, D = S::D, R = S::R, NT = S::NT, TJ = S::TJ;
-    constexpr int ROWS = S::ROWS;
-    // dynamic shared memory: the runtime aligns it to at least 128 bytes (no static shared
-    // variables precede it in this kernel); every pointer below stays in the shared window
-    extern __shared__ __align__(128) unsigned char smem[];
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
-    int* s_fail = reinterpret_cast<int*>(smem + 8 * NS);
-    float* lut = reinterpret_cast<float*>(smem + 128);
-    float2* tab = reinterpret_cast<float2*>(smem + 128 + S::LUT_BYTES);
-    float* const F0 = reinterpret_cast<float*>(smem + S::HEAD + S::GUARD);
-    unsigned char* const C0 = smem + S::HEAD + S::FSPAN;
-
-    const Geo& g = a.g;
-    const int tid = threadIdx.x;
-    const int ty = tid / G;
-    const int gi = tid - ty * G;
-    const int jj = 4 * gi;
-    const int j0 = blockIdx.x * TJ;
-    const int y0 = blockIdx.y * TY;
-    const int b = blockIdx.z;
-    const int NX = g.NX;
-    const int y = y0 - K + ty;  // interior y of this thread's row (may lie in a ghost band)
-    const int row0 = 2 * (y0 + HY - K);  // first staged row of the TMA box (padded coordinates)
-    const int c0 = a.first_colour;
-    const float4 glo4 = make_float4(a.glo, a.glo, a.glo, a.glo);
-    const float4 ghi4 = make_float4(a.ghi, a.ghi, a.ghi, a.ghi);
-
-    if (tid == 0) {
-        for (int s = 0; s < NS; ++s) mbar_init(&bar[s], 1);
-        fence_mbar_init();
-        *s_fail = 0;
-    }
-    if (KIND == TF_KIND_ANISOTROPIC)
-        for (int i = tid; i < 256; i += NT) lut[i] = op.divisor[i];
-    if (KIND == TF_KIND_MULTIPHASE)
-        for (int i = tid; i < 32 * 32; i += NT) lut[i] = op.face[i];
-    fill_division_table(tab, tid);
-    for (int s = 0; s < NS; ++s) {
-        float* f = F0 + s * (S::SLOT / 4);
-        for (int i = tid; i < S::GUARD / 4; i += NT) {
-            f[-1 - i] = 0.0f;
-            f[S::FBYTES / 4 + i] = 0.0f;
-        }
-    }
-    __syncthreads();
-
-    auto issue = [&](int x) {
-        const int s = x % NS;
-        mbar_arrive_expect_tx(&bar[s], S::FBYTES + S::CBYTES);
-        tma_load_3d(F0 + s * (S::SLOT / 4), &tmf, &bar[s], j0, row0, b * NX + x);
-        tma_load_3d(C0 + s * S::SLOT, &tmc, &bar[s], j0, row0, b * NX + x);
-    };
-    if (tid == 0)
-        for (int x = 0; x < D && x < NX; ++x) issue(x);
-
-    // own cells by relative colour (V0, V1) and their codes (K0, K1); ring index = plane % R.
-    // Plane -1 (ring slot R-1 until plane R-1 arrives) and plane NX are the Dirichlet ghost
-    // planes 2*bc, so x-neighbours need no boundary selects.
-    float4 V0[R], V1[R];
-    uint32_t K0[R], K1[R];
-#pragma unroll
-    for (int r = 0; r < R; ++r) {
-        V0[r] = V1[r] = glo4;
-        K0[r] = K1[r] = 0u;
-    }
-
-    const bool interior_group = gi >= 1 && gi < G - 1;
-    const bool py = a.periodic & TF_PERIODIC_Y, pz = a.periodic & TF_PERIODIC_Z;
-    const int total = NX + K;
-    for (int t0 = 0; t0 < total; t0 += R) {
-#pragma unroll
-        for (int i = 0; i < R; ++i) {
-            const int t = t0 + i;
-            if (t < total) {
-                if (tid == 0 && t + D < NX) issue(t + D);
-                if (t < NX) {
-                    const int slot = t % NS;
-                    if (!mbar_wait_bounded(&bar[slot], (t / NS) & 1)) *s_fail = 1;
-                    const float* Fs = F0 + slot * (S::SLOT / 4);
-                    const unsigned char* Cs = C0 + slot * S::SLOT;
-                    const float4 e4 = ld4(Fs + (2 * ty) * WJ + jj);
-                    const float4 o4 = ld4(Fs + (2 * ty + 1) * WJ + jj);
-                    const uint32_t ce = ld_u32(Cs + (2 * ty) * WJC + jj);
-                    const uint32_t co = ld_u32(Cs + (2 * ty + 1) * WJC + jj);
-                    const bool even0 = ((t + y + c0) & 1) == 0;  // even-z cells have relative colour 0
-                    V0[i] = even0 ? e4 : o4;
-                    V1[i] = even0 ? o4 : e4;
-                    K0[i] = even0 ? ce : co;
-                    K1[i] = even0 ? co : ce;
-                } else if (t == NX) {
-                    V0[i] = V1[i] = ghi4;
-                }
-#pragma unroll
-                for (int s = 1; s <= K; ++s) {
-                    const int p = t - s;
-                    const int ip = (i - s + 2 * R) % R;
-                    const int ipn = (i - s + 1 + 2 * R) % R;
-                    const int ipp = (i - s - 1 + 2 * R) % R;
-                    // rows [s, ROWS - s) form the region of half-sweep s: it shrinks by one row per
-                    // half-sweep so the tile interior is exact after K of them
-                    if (p >= 0 && p < NX && ty >= s && ty < ROWS - s) {
-                        float* Fp = F0 + (p % NS) * (S::SLOT / 4);
-                        const unsigned char* Cp = C0 + (p % NS) * S::SLOT;
-                        const bool at_lo = p == 0, at_hi = p == NX - 1;
-                        // relative colour (s-1)&1 updates; even-z cells hold relative colour (p+y+c0)&1
-                        const int q = ((p + y + c0) & 1) ^ ((s - 1) & 1);  // half-row type being updated
-                        const int row_up = 2 * (ty + 1) + q, row_dn = 2 * (ty - 1) + q, row_me = 2 * ty + q;
-                        const int row_ot = 2 * ty + (q ^ 1);
-                        if (((s - 1) & 1) == 0) {
-                            const uint32_t cxp = at_hi ? K0[ip] : K1[ipn], cxm = at_lo ? K0[ip] : K1[ipp];
-                            stage_update<KIND>(V0[ip], V1[ipn], V1[ipp], V1[ip], K0[ip], cxp, cxm, K1[ip], Fp, Cp,
-                                               row_up, row_dn, row_me, row_ot, jj, q, WJ, WJC, at_lo, at_hi,
-                                               a, lut, tab);
-                        } else {
-                            const uint32_t cxp = at_hi ? K1[ip] : K0[ipn], cxm = at_lo ? K1[ip] : K0[ipp];
-                            stage_update<KIND>(V1[ip], V0[ipn], V0[ipp], V0[ip], K1[ip], cxp, cxm, K0[ip], Fp, Cp,
-                                               row_up, row_dn, row_me, row_ot, jj, q, WJ, WJC, at_lo, at_hi,
-                                               a, lut, tab);
-                        }
-                    }
-                }
-                // write back plane t-K from registers
-                const int pw = t - K;
-                const int iw = (i - K + 2 * R) % R;
-                if (pw >= 0 && interior_group && ty >= K && ty < K + TY && y < g.NY) {
-                    const bool even0 = ((pw + y + c0) & 1) == 0;
-                    const float4 ev = even0 ? V0[iw] : V1[iw];
-                    const float4 od = even0 ? V1[iw] : V0[iw];
-                    const int j = j0 + 4 * (gi - 1);
-                    float* outp = a.out + (long long)b * g.vol_f + (long long)pw * g.plane_f;
-#pragma unroll
-                    for (int q = 0; q < 2; ++q) {
-                        const float4 v = q ? od : ev;
-                        const int nj = half_len(g.NZ, q);
-                        if (j >= nj) continue;
-                        float* rowp = outp + (long long)(y + HY) * g.row_f + q * g.ZH + HJ;
-                        if (j + 4 <= nj) {
-                            st4(rowp + j, v);
-                        } else {
-                            for (int c = 0; c < nj - j; ++c) rowp[j + c] = comp(v, c);
-                        }
-                        if (py || pz) {
-                            const int hz = g.NZ >> 1;
-                            if ((hz & 3) == 0) {
-                                // periodic ghost copies as whole aligned groups
-                                const bool yb = py && (y < HY || y >= g.NY - HY);
-                                const int ys = y < HY ? y + g.NY : y - g.NY;
-                                const bool zb = pz && (j == 0 || j == hz - 4);
-                                const int jz = j == 0 ? hz : -4;
-                                float* rows_ = outp + (long long)(ys + HY) * g.row_f + q * g.ZH + HJ;
-                                if (yb) st4(rows_ + j, v);
-                                if (zb) st4(rowp + jz, v);
-                                if (yb && zb) st4(rows_ + jz, v);
-                            } else if ((py && (y < HY || y >= g.NY - HY)) || (pz && (j < HJ || j + 4 > hz - HJ))) {
-                                ghost_copies_scalar(outp, g.row_f, g.ZH, g.NY, g.NZ, y, q, j, nj, v, py);
-                            }
-                        }
-                    }
-                }
-                fence_proxy_async_smem();
-                __syncthreads();
-                if (*s_fail) {
-                    if (tid == 0) {
-                        for (int x = t + 1; x < t + 1 + D && x < NX; ++x) mbar_wait_bounded(&bar[x % NS], (x / NS) & 1);
-                        if (a.err) atomicExch(a.err, TF_ERR_TIMEOUT);
-                    }
-                    return;
-                }
-            }
-        }
-    }
-}
-
-// ------------------------------------------------------------------------------ host side
-template <int KIND, int TY, int TZ, int K>
-static int launch_stream(const tf_geom& gg, const tf_operator& op, const float* in, float* out, const uint8_t* code,
-                         int first_colour, int32_t* err, cudaStream_t st) {
-    using S = StreamShape<TY, TZ, K>;
-    CUtensorMap tmf, tmc;
-    int rc = encode_map_3d(&tmf, in, 4, gg.zh, 2 * gg.yp, (long long)gg.batch * gg.nx, (long long)gg.zh * 4,
-                           (long long)gg.zh * 4 * 2 * gg.yp, S::WJ, 2 * S::ROWS);
-    if (rc) return rc;
-    rc = encode_map_3d(&tmc, code, 1, gg.zhc, 2 * gg.yp, (long long)gg.batch * gg.nx, gg.zhc,
-                       (long long)gg.zhc * 2 * gg.yp, S::WJC, 2 * S::ROWS);
-    if (rc) return rc;
-    static bool attr_set = false;
-    auto kern = k_stream<KIND, TY, TZ, K>;
-    if (!attr_set) {
-        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM) != cudaSuccess)
-            return TF_ERR_CUDA;
-        attr_set = true;
-    }
-    const SweepArgs a = make_args(make_geo(gg), op, out, first_colour, K, err);
-    dim3 grid((gg.nz + TZ - 1) / TZ, (gg.ny + TY - 1) / TY, gg.batch);
-    kern<<<grid, S::NT, S::SMEM, st>>>(tmf, tmc, a, op);
-    note_launch();
-    return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
-}
-
-template <int KIND, int TY, int TZ>
-static int dispatch_k(const tf_geom& g, const tf_operator& op, const float* in, float* out, const uint8_t* code,
-                      int first_colour, int n_half, int32_t* err, cudaStream_t st) {
-    switch (n_half) {
-        case 1: return launch_stream<KIND, TY, TZ, 1>(g, op, in, out, code, first_colour, err, st);
-        case 2: return launch_stream<KIND, TY, TZ, 2>(g, op, in, out, code, first_colour, err, st);
-        case 3: return launch_stream<KIND, TY, TZ, 3>(g, op, in, out, code, first_colour, err, st);
-        case 4: return launch_stream<KIND, TY, TZ, 4>(g, op, in, out, code, first_colour, err, st);
-    }
-    return TF_ERR_ARG;
-}
-
-// Tile shapes (op.tile): 0 = 16x64, 1 = 16x128, 2 = 32x64 (rows x z-cells). The multiphase and
-// anisotropic operators use shape 0.
-template <int KIND>
-static int dispatch_kind(const tf_geom& g, const tf_operator& op, const float* in, float* out, const uint8_t* code,
-                         int first_colour, int n_half, int32_t* err, cudaStream_t st) {
-    if (KIND == TF_KIND_BINARY && op.tile == 1)
-        return dispatch_k<KIND, 16, 128>(g, op, in, out, code, first_colour, n_half, err, st);
-    if (KIND == TF_KIND_BINARY && op.tile == 2)
-        return dispatch_k<KIND, 32, 64>(g, op, in, out, code, first_colour, n_half, err, st);
-    return dispatch_k<KIND, 16, 64>(g, op, in, out, code, first_colour, n_half, err, st);
-}
+int sweep_tiled_bin(const tf_geom&, const tf_operator&, const float*, float*, const uint8_t*, const float*, int, int,
+                    int32_t*, cudaStream_t);
+int sweep_tiled_aniso(const tf_geom&, const tf_operator&, const float*, float*, const uint8_t*, const float*, int, int,
+                      int32_t*, cudaStream_t);
+int sweep_tiled_mp(const tf_geom&, const tf_operator&, const float*, float*, const uint8_t*, const float*, int, int,
+                   int32_t*, cudaStream_t);
 
 int sweep_tiled(const tf_geom& g, const tf_operator& op, const float* in, float* out, const uint8_t* code,
-                int first_colour, int n_half, int32_t* err, cudaStream_t st) {
+                const float* rhs, int first_colour, int n_half, int32_t* err, cudaStream_t st) {
     switch (op.kind) {
-        case TF_KIND_BINARY: return dispatch_kind<TF_KIND_BINARY>(g, op, in, out, code, first_colour, n_half, err, st);
-        case TF_KIND_ANISOTROPIC:
-            return dispatch_kind<TF_KIND_ANISOTROPIC>(g, op, in, out, code, first_colour, n_half, err, st);
-        case TF_KIND_MULTIPHASE:
-            return dispatch_kind<TF_KIND_MULTIPHASE>(g, op, in, out, code, first_colour, n_half, err, st);
+        case TF_KIND_BINARY: return sweep_tiled_bin(g, op, in, out, code, rhs, first_colour, n_half, err, st);
+        case TF_KIND_ANISOTROPIC: return sweep_tiled_aniso(g, op, in, out, code, rhs, first_colour, n_half, err, st);
+        case TF_KIND_MULTIPHASE: return sweep_tiled_mp(g, op, in, out, code, rhs, first_colour, n_half, err, st);
     }
     return TF_ERR_ARG;
 }

@@ -19,7 +19,7 @@
 namespace tf {
 
 // ------------------------------------------------------------------------------ plain kernel
-template <int KIND>
+template <int KIND, bool RHS>
 __global__ void __launch_bounds__(256) k_plain(float* __restrict__ f, const uint8_t* __restrict__ code,
                                                const SweepArgs a, const __grid_constant__ tf_operator op, int colour) {
     __shared__ float lut[32 * 32];
@@ -69,8 +69,10 @@ __global__ void __launch_bounds__(256) k_plain(float* __restrict__ f, const uint
         cym = ld_code(crow - g.row_c + j);
         z_codes(q, ld_code(corow + j), q ? corow[j + 4] : corow[j - 1], czp, czm);
     }
-    const float4 nv = update4<KIND>(c, xp, xm, yp, ym, zp, zm, cc, cxp, cxm, cyp, cym, czp, czm, x == 0,
-                                    x == g.NX - 1, a.omega, a.ky, a.kz, lut, tab);
+    float4 rv = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (RHS) rv = *reinterpret_cast<const float4*>(a.rhs + base + q * g.ZH + HJ + j);
+    const float4 nv = update4<KIND, RHS>(c, xp, xm, yp, ym, zp, zm, cc, cxp, cxm, cyp, cym, czp, czm, x == 0,
+                                         x == g.NX - 1, a.omega, a.ky, a.kz, lut, tab, rv);
     float* dst = f + base + q * g.ZH + HJ + j;
     for (int i = 0; i < 4 && j + i < nj; ++i) dst[i] = comp(nv, i);
 }
@@ -127,22 +129,28 @@ SweepArgs make_args(const Geo& g, const tf_operator& op, float* out, int first_c
     a.g = g; a.out = out; a.omega = op.omega; a.glo = op.ghost_lo; a.ghi = op.ghost_hi;
     a.ky = op.ky; a.kz = op.kz; a.first_colour = first_colour & 1; a.n_half = n_half; a.err = err;
     a.periodic = op.periodic;
+    a.rhs = nullptr;
     return a;
 }
 
-int sweep_plain(const tf_geom& gg, const tf_operator& op, float* f, const uint8_t* code, int colour,
-                cudaStream_t st) {
+int sweep_plain(const tf_geom& gg, const tf_operator& op, float* f, const uint8_t* code, const float* rhs,
+                int colour, cudaStream_t st) {
     const Geo g = make_geo(gg);
-    const SweepArgs a = make_args(g, op, f, colour, 1, nullptr);
+    SweepArgs a = make_args(g, op, f, colour, 1, nullptr);
+    a.rhs = rhs;
     const int gmax = (half_len(g.NZ, 0) + 3) >> 2;
     dim3 block(gmax >= 128 ? 128 : (gmax >= 32 ? 64 : 32));
     dim3 grid((gmax + block.x - 1) / block.x, g.NY, g.B * g.NX);
+#define TF_PLAIN(K)                                                                        \
+    (rhs ? k_plain<K, true><<<grid, block, 0, st>>>(f, code, a, op, colour)                  \
+         : k_plain<K, false><<<grid, block, 0, st>>>(f, code, a, op, colour))
     switch (op.kind) {
-        case TF_KIND_BINARY: k_plain<TF_KIND_BINARY><<<grid, block, 0, st>>>(f, code, a, op, colour); break;
-        case TF_KIND_ANISOTROPIC: k_plain<TF_KIND_ANISOTROPIC><<<grid, block, 0, st>>>(f, code, a, op, colour); break;
-        case TF_KIND_MULTIPHASE: k_plain<TF_KIND_MULTIPHASE><<<grid, block, 0, st>>>(f, code, a, op, colour); break;
+        case TF_KIND_BINARY: TF_PLAIN(TF_KIND_BINARY); break;
+        case TF_KIND_ANISOTROPIC: TF_PLAIN(TF_KIND_ANISOTROPIC); break;
+        case TF_KIND_MULTIPHASE: TF_PLAIN(TF_KIND_MULTIPHASE); break;
         default: return TF_ERR_ARG;
     }
+#undef TF_PLAIN
     note_launch();
     if (cudaGetLastError() != cudaSuccess) return TF_ERR_CUDA;
     if (op.periodic) return refresh_ghosts(gg, op.periodic, f, st);

@@ -11,6 +11,7 @@ struct SweepArgs {
     float omega, glo, ghi, ky, kz;
     int first_colour, n_half, periodic;
     int32_t* err;
+    const float* rhs;  // right-hand side of a correction solve (split layout), or null
 };
 
 SweepArgs make_args(const Geo& g, const tf_operator& op, float* out, int first_colour, int n_half, int32_t* err);
@@ -49,9 +50,10 @@ static __device__ __noinline__ float4 tiny_quotients(float4 sum, float4 n, float
 // chains overlap: sum in the order of taufactor.py:97-102 (x+1, x-1, y+1, y-1, z+1, z-1),
 // exact division by the neighbour count (table entry (n, RN(1/n)); code 0 -> (1, 0) gives the
 // reference's sum/inf = signed zero), then inc = q - c; inc *= omega; c += inc (:177-181).
+template <bool RHS>
 __device__ __forceinline__ float4 update4_binary(float4 c, const float4& xp, const float4& xm, const float4& yp,
                                                  const float4& ym, const float4& zp, const float4& zm, uint32_t cc,
-                                                 float omega, const float2* tab) {
+                                                 float omega, const float2* tab, const float4& rv) {
     float4 s, n, r, q;
 #define TF_S1(L) s.L = __fadd_rn(xp.L, xm.L);
 #define TF_S2(L) s.L = __fadd_rn(s.L, yp.L);
@@ -59,6 +61,11 @@ __device__ __forceinline__ float4 update4_binary(float4 c, const float4& xp, con
 #define TF_S4(L) s.L = __fadd_rn(s.L, zp.L);
 #define TF_S5(L) s.L = __fadd_rn(s.L, zm.L);
     TF_LANES(TF_S1) TF_LANES(TF_S2) TF_LANES(TF_S3) TF_LANES(TF_S4) TF_LANES(TF_S5)
+    if (RHS) {
+#define TF_S6(L) s.L = __fadd_rn(s.L, rv.L);
+        TF_LANES(TF_S6)
+#undef TF_S6
+    }
     const float2 t0 = tab[cc & 0xffu], t1 = tab[(cc >> 8) & 0xffu], t2 = tab[(cc >> 16) & 0xffu], t3 = tab[cc >> 24];
     n = make_float4(t0.x, t1.x, t2.x, t3.x);
     r = make_float4(t0.y, t1.y, t2.y, t3.y);
@@ -93,13 +100,14 @@ __device__ __forceinline__ float4 update4_binary(float4 c, const float4& xp, con
 //   lut      anisotropic: divisor per code; multiphase: face table [32][32];
 //   tab      binary: (n, RN(1/n)) per code n = 1..8; entry 0 = (1, 0) makes the quotient of a
 //            frozen voxel (the reference's inf divisor) a signed zero without a branch.
-template <int KIND>
+template <int KIND, bool RHS = false>
 __device__ __forceinline__ float4 update4(float4 c, const float4& xp, const float4& xm, const float4& yp,
                                           const float4& ym, const float4& zp, const float4& zm, uint32_t cc,
                                           uint32_t cxp, uint32_t cxm, uint32_t cyp, uint32_t cym, uint32_t czp,
                                           uint32_t czm, bool at_lo, bool at_hi, float omega, float ky, float kz,
-                                          const float* lut, const float2* tab) {
-    if (KIND == TF_KIND_BINARY) return update4_binary(c, xp, xm, yp, ym, zp, zm, cc, omega, tab);
+                                          const float* lut, const float2* tab,
+                                          const float4& rv = make_float4(0.f, 0.f, 0.f, 0.f)) {
+    if (KIND == TF_KIND_BINARY) return update4_binary<RHS>(c, xp, xm, yp, ym, zp, zm, cc, omega, tab, rv);
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         const float ci = comp(c, i);
@@ -120,6 +128,7 @@ __device__ __forceinline__ float4 update4(float4 c, const float4& xp, const floa
             sum = __fadd_rn(comp(xp, i), comp(xm, i));
             sum = __fadd_rn(sum, __fmul_rn(ky, __fadd_rn(comp(yp, i), comp(ym, i))));
             sum = __fadd_rn(sum, __fmul_rn(kz, __fadd_rn(comp(zp, i), comp(zm, i))));
+            if (RHS) sum = __fadd_rn(sum, comp(rv, i));
             quot = quotient(sum, lut[byte_of(cc, i)]);
         } else {
             // taufactor.py:607-612 (products first, then left-to-right sum) and the factor of
@@ -137,6 +146,7 @@ __device__ __forceinline__ float4 update4(float4 c, const float4& xp, const floa
             sum = __fadd_rn(sum, __fmul_rn(comp(ym, i), fym));
             sum = __fadd_rn(sum, __fmul_rn(comp(zp, i), fzp));
             sum = __fadd_rn(sum, __fmul_rn(comp(zm, i), fzm));
+            if (RHS) sum = __fadd_rn(sum, comp(rv, i));
             float div = __fadd_rn(fxm, fxp);
             div = __fadd_rn(div, fym);
             div = __fadd_rn(div, fyp);

@@ -27,7 +27,7 @@ from timeit import default_timer as timer
 import numpy as np
 import torch
 
-from . import _capi
+from . import _capi, autotune
 from ._capi import (TF_KIND_ANISOTROPIC, TF_KIND_BINARY, TF_KIND_MULTIPHASE, TF_MAX_PHASES,
                     TF_PERIODIC_Y, TF_PERIODIC_Z, TfGeom, TfOperator, check)
 from .percolation import spans_x
@@ -65,6 +65,7 @@ class SORSolver:
         phase, mask = self._phase_indices()
         self.vol_x = mask.mean(axis=(2, 3), dtype=np.float64)
         self._op = self._operator(float(omega))
+        autotune.apply(self, *autotune.default_config(self))
         self._build(phase)
         self.converged = False
         self.old_tau = 0
@@ -113,6 +114,7 @@ class SORSolver:
             self._flux_dev = torch.empty((self.batch_size, max(self.Nx - 1, 1)), dtype=torch.float64, device=dev)
             self._csum_dev = torch.empty((self.batch_size, self.Nx), dtype=torch.float64, device=dev)
         self._cur, self._other = self._fa, self._fb
+        self._field64 = None
 
     def _pack(self):
         with torch.cuda.device(self.device):
@@ -122,6 +124,7 @@ class SORSolver:
 
     def reset(self):
         """Restart the solve from the initial linear field, keeping the device buffers."""
+        self._field64 = None
         self._pack()
         self._cur, self._other = self._fa, self._fb
         self.converged = False
@@ -132,10 +135,60 @@ class SORSolver:
     def _stream(self):
         return torch.cuda.current_stream(self.device).cuda_stream
 
+    def tune(self, half_sweeps: int = 48) -> dict:
+        """Pick the fastest tile shape / half-sweeps per launch for these volumes (results unchanged)."""
+        return autotune.tune(self, half_sweeps)
+
+    def refine(self, tol: float = 1e-10, max_outer: int = 12, inner_half_sweeps: int | None = None):
+        """FP64 defect correction of the current field; returns the relative residual history.
+
+        Keeps the solution in float64, forms r = b - A c in float64 on the device, solves A e = r
+        with the float32 sweeps (right-hand side r, homogeneous Dirichlet faces, same omega) and
+        adds e in float64, until max over volumes of ||r|| / ||b|| < tol. The reference has no
+        such step (it iterates in float32 only, taufactor.py:172-182). Afterwards the metrics
+        (D_eff, tau, flux_1d, c_x, tau_x) come from the float64 field and the float32 field holds
+        its rounding.
+        """
+        g, lib, dev = self._geom, self._lib, self.device
+        gp, st = C.byref(g), None
+        op0 = TfOperator.from_buffer_copy(self._op)
+        op0.ghost_lo = op0.ghost_hi = 0.0
+        n_inner = inner_half_sweeps or max(400, 2 * (self.iter or 200))
+        with torch.cuda.device(dev):
+            st = self._stream()
+            c64 = torch.empty(g.field_elems, dtype=torch.float64, device=dev)
+            check(lib.tf_widen_f64(gp, _ptr(self._cur), _ptr(c64), st), "tf_widen_f64")
+            rhs = torch.zeros(g.field_elems, dtype=torch.float32, device=dev)
+            ea = torch.zeros_like(rhs)
+            eb = torch.zeros_like(rhs)
+            r2 = torch.empty((self.batch_size, self.Nx), dtype=torch.float64, device=dev)
+            b2 = torch.empty_like(r2)
+            hist = []
+            for outer in range(max_outer + 1):
+                check(lib.tf_residual_f64(gp, C.byref(self._op), _ptr(c64), _ptr(self._code), _ptr(rhs), _ptr(r2),
+                                          _ptr(b2), st), "tf_residual_f64")
+                bn = torch.sqrt(b2.sum(dim=1)).clamp_min(1e-300)
+                rel = float((torch.sqrt(r2.sum(dim=1)) / bn).max().item())
+                hist.append(rel)
+                if rel < tol or outer == max_outer:
+                    break
+                ea.zero_()
+                in_b = C.c_int(0)
+                check(lib.tf_advance_rhs(gp, C.byref(op0), _ptr(ea), _ptr(eb), _ptr(self._code), _ptr(rhs), 0,
+                                         n_inner, _ptr(self._err), C.byref(in_b), st), "tf_advance_rhs")
+                check(lib.tf_axpy_f64(gp, _ptr(c64), _ptr(eb if in_b.value else ea), st), "tf_axpy_f64")
+            check(lib.tf_narrow_f64(gp, C.byref(self._op), _ptr(c64), _ptr(self._cur), st), "tf_narrow_f64")
+        self._field64 = c64
+        self.residual_history = hist
+        self.tau, _ = self.compute_metrics()
+        self.tau = np.where(self.tau == 0, np.inf, self.tau)
+        return hist
+
     def _advance(self, n: int):
         """n half-sweeps (reference iterations) starting at colour iter % 2."""
         if n <= 0:
             return
+        self._field64 = None
         in_b = C.c_int(0)
         ev = self.event_log
         if ev is not None:
@@ -154,11 +207,19 @@ class SORSolver:
         self.iter += n
 
     def _layer_means(self):
-        """float64 per-layer means of the x-flux [B,Nx-1] and of the field [B,Nx]."""
+        """float64 per-layer means of the x-flux [B,Nx-1] and of the field [B,Nx].
+
+        Taken from the float64 field once refine() has produced one, else from the float32 field.
+        """
         with torch.cuda.device(self.device):
-            check(self._lib.tf_layer_sums(C.byref(self._geom), C.byref(self._op), _ptr(self._cur), _ptr(self._code),
-                                          _ptr(self._flux_dev), _ptr(self._csum_dev), self._stream()),
-                  "tf_layer_sums")
+            if self._field64 is not None:
+                check(self._lib.tf_layer_sums_f64(C.byref(self._geom), C.byref(self._op), _ptr(self._field64),
+                                                  _ptr(self._code), _ptr(self._flux_dev), _ptr(self._csum_dev),
+                                                  self._stream()), "tf_layer_sums_f64")
+            else:
+                check(self._lib.tf_layer_sums(C.byref(self._geom), C.byref(self._op), _ptr(self._cur),
+                                              _ptr(self._code), _ptr(self._flux_dev), _ptr(self._csum_dev),
+                                              self._stream()), "tf_layer_sums")
             flux = self._flux_dev.cpu().numpy()
             csum = self._csum_dev.cpu().numpy()
             err = int(self._err.item())
@@ -221,11 +282,13 @@ class SORSolver:
         self.tau[self.tau == 0] = np.inf
         return True
 
-    def solve(self, iter_limit=10000, verbose=True, conv_crit=1e-2, plot_interval=10):
+    def solve(self, iter_limit=10000, verbose=True, conv_crit=1e-2, plot_interval=10, refine=False):
         """Run half-sweeps until converged or iter_limit (taufactor.py:156-191).
 
         Half-sweeps between two checks run as fused multi-half-sweep launches with no host
-        synchronisation; the check every 100 half-sweeps reads the layer sums back.
+        synchronisation; the check every 100 half-sweeps reads the layer sums back. With
+        ``refine=True`` (no reference counterpart) the converged field is then corrected in
+        float64 (see refine()) and the returned metrics are those of the refined field.
         """
         if verbose:
             torch.cuda.reset_peak_memory_stats(device=self.device)
@@ -237,6 +300,8 @@ class SORSolver:
             self._advance(n)
             if self.iter % 100 == 0:
                 self.converged = self.check_convergence(verbose, conv_crit, plot_interval)
+        if refine:
+            self.refine(**(refine if isinstance(refine, dict) else {}))
         torch.cuda.synchronize(self.device)
         self.walltime = timer() - start
         self._end_simulation(self.iter, verbose)
