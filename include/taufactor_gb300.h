@@ -168,6 +168,62 @@ int tf_repack(const tf_geom* g, const tf_operator* op, const float* padded_dev, 
  * (taufactor.py:177). */
 int tf_check_small_division(int n, uint64_t* bad_dev, void* stream);
 
+/* ---------------------------------------------------------------- batched uneven solves
+ * Many binary volumes (Solver / PeriodicSolver operators) of different shapes advance in the
+ * same launches; each volume keeps its own buffers (tf_geometry with batch = 1) and its own
+ * convergence state, evaluated on the device with the reference's rule (taufactor.py:109-153).
+ * No reference counterpart as an API: the reference batches only same-shape volumes, which
+ * converge together (taufactor.py:30-31, :143). */
+#define TF_BATCH_ACTIVE 0
+#define TF_BATCH_CONVERGED 1
+#define TF_BATCH_NEEDS_HOST 2 /* a layer flux is 0 and percolation is unknown: host decides */
+
+typedef struct tf_batch_state { /* device arrays of n_vol entries unless noted */
+    int32_t* status;            /* TF_BATCH_*                                                 */
+    int32_t* perc;              /* 0 unknown, 1 spanning path, 2 none (set by the host)       */
+    int32_t* conv_iter;         /* half-sweeps at convergence (or at the pause)               */
+    int32_t* conv_parity;       /* 1 if the volume's final field is in its buffer B           */
+    double* old_tau;            /* tau of the previous check (starts at 0)                    */
+    double* tau;                /* last tau, relative flux spread and D_rel                   */
+    double* rel;
+    double* d_rel;
+    int32_t* iter_base;         /* one int: half-sweeps completed before the current graph    */
+} tf_batch_state;
+
+/* Bytes of the device descriptor table for n_vol volumes. */
+size_t tf_batch_desc_bytes(int n_vol);
+
+/* Tile shape and half-sweeps per launch of the batched sweep. */
+void tf_batch_tile(int* tile_y, int* tile_z, int* half_sweeps);
+
+/* Fill the descriptor table (device memory, tf_batch_desc_bytes) from per-volume geometry,
+ * operator, buffers (field A holds the current field), layer-sum offsets (flux arena offset of
+ * plane 0; csum arena likewise) and mean conductive fraction d_mean (tau = d_mean / D_rel).
+ * Synchronous (copies the table to the device). */
+int tf_batch_describe(int n_vol, const tf_geom* geoms, const tf_operator* ops, float* const* field_a,
+                      float* const* field_b, const uint8_t* const* codes, const int64_t* flux_off,
+                      const int64_t* csum_off, const double* d_mean, int32_t* err_dev, void* desc_dev);
+
+/* Advance every active volume by the batch's half-sweeps per launch (colour 0 first, so the
+ * completed half-sweeps must stay a multiple of it). work_dev: int32 pairs (volume, tile) with
+ * tile = ty * tiles_z + tz. parity 0 reads buffers A and writes B, 1 the reverse. */
+int tf_batch_advance(const void* desc_dev, const int32_t* work_dev, int n_work, const int32_t* status_dev,
+                     int parity, void* stream);
+
+/* Per-plane float64 flux / field sums of every active volume (tf_layer_sums per volume) into
+ * the arenas; planes_dev: int32 pairs (volume, x). cur_in_b: the current fields are in B. */
+int tf_batch_layer_sums(const void* desc_dev, const int32_t* planes_dev, int n_planes,
+                        const int32_t* status_dev, int cur_in_b, double* flux_dev, double* csum_dev,
+                        void* stream);
+
+/* The reference's convergence decision for every active volume from its layer fluxes; the
+ * current iteration is *iter_base + 100 * (interval + 1). */
+int tf_batch_check(const void* desc_dev, int n_vol, const double* flux_dev, tf_batch_state state,
+                   double conv_crit, int interval, int cur_in_b, void* stream);
+
+/* *iter_base_dev += half_sweeps (stream-ordered). */
+int tf_batch_tick(int32_t* iter_base_dev, int half_sweeps, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -6,9 +6,10 @@ Drop-in for the through-transport solvers of tldr-group/taufactor v1.2.1
 surface. The sweeps run as hand-written CUDA kernels of ``lib/libtaufactor_gb300.so`` through
 its C ABI (``include/taufactor_gb300.h``).
 """
+from .batch import BatchSolve
 from .solvers import (AnisotropicSolver, MultiPhaseSolver, PeriodicMultiPhaseSolver, PeriodicSolver,
                       SORSolver, Solver, ThroughTransportSolver)
 
 __all__ = ["Solver", "PeriodicSolver", "AnisotropicSolver", "MultiPhaseSolver", "PeriodicMultiPhaseSolver",
-           "SORSolver", "ThroughTransportSolver"]
+           "SORSolver", "ThroughTransportSolver", "BatchSolve"]
 __version__ = "0.1.0"

@@ -20,8 +20,10 @@ TF_MAX_HALF_SWEEPS = 4
 EXPORTS = (
     "tf_version", "tf_status_string", "tf_launch_count", "tf_geometry", "tf_pack", "tf_advance",
     "tf_layer_sums", "tf_unpack", "tf_repack", "tf_check_small_division", "tf_advance_rhs", "tf_widen_f64",
-    "tf_narrow_f64", "tf_axpy_f64", "tf_residual_f64", "tf_layer_sums_f64",
+    "tf_narrow_f64", "tf_axpy_f64", "tf_residual_f64", "tf_layer_sums_f64", "tf_batch_desc_bytes", "tf_batch_tile",
+    "tf_batch_describe", "tf_batch_advance", "tf_batch_layer_sums", "tf_batch_check", "tf_batch_tick",
 )
+TF_BATCH_ACTIVE, TF_BATCH_CONVERGED, TF_BATCH_NEEDS_HOST = 0, 1, 2
 
 
 class TfGeom(C.Structure):
@@ -37,6 +39,12 @@ class TfOperator(C.Structure):
                 ("n_phases", C.c_int32), ("tile", C.c_int32), ("k_max", C.c_int32),
                 ("divisor", C.c_float * 256), ("face", C.c_float * 1024),
                 ("conductive", C.c_uint8 * 32)]
+
+
+class TfBatchState(C.Structure):
+    _fields_ = [("status", C.c_void_p), ("perc", C.c_void_p), ("conv_iter", C.c_void_p),
+                ("conv_parity", C.c_void_p), ("old_tau", C.c_void_p), ("tau", C.c_void_p), ("rel", C.c_void_p),
+                ("d_rel", C.c_void_p), ("iter_base", C.c_void_p)]
 
 
 class TfError(RuntimeError):
@@ -82,6 +90,13 @@ def load():
         "tf_axpy_f64": (i32, [G, vp, vp, vp]),
         "tf_residual_f64": (i32, [G, O, vp, vp, vp, vp, vp, vp]),
         "tf_layer_sums_f64": (i32, [G, O, vp, vp, vp, vp, vp]),
+        "tf_batch_desc_bytes": (C.c_size_t, [i32]),
+        "tf_batch_tile": (None, [C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+        "tf_batch_describe": (i32, [i32, G, O, vp, vp, vp, vp, vp, vp, vp, vp]),
+        "tf_batch_advance": (i32, [vp, vp, i32, vp, i32, vp]),
+        "tf_batch_layer_sums": (i32, [vp, vp, i32, vp, i32, vp, vp, vp]),
+        "tf_batch_check": (i32, [vp, i32, vp, TfBatchState, C.c_double, i32, i32, vp]),
+        "tf_batch_tick": (i32, [vp, i32, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -1,0 +1,316 @@
+"""Batched solve of many binary volumes of uneven shapes on one GPU.
+
+The reference batches only volumes of one shape along a leading axis, and the whole batch
+iterates until its slowest member converges (taufactor/taufactor.py:30-31, :143). Here every
+volume keeps its own shape, buffers and convergence state:
+
+* one launch of the fused sweep advances all still-active volumes by 4 half-sweeps (CTAs of
+  converged volumes return at once);
+* every 100 half-sweeps the per-volume layer sums and the reference's convergence decision
+  (taufactor.py:109-153, :293-331) run on the device and set a per-volume status;
+* two such check intervals (50 sweep launches, two layer-sum and two decision launches) are
+  captured once as a CUDA graph and replayed; the host reads the status flags between replays
+  and only steps in for a volume whose layer flux is exactly zero (the percolation test of
+  taufactor.py:318-327 runs on the host, as in the reference).
+
+Each volume's result equals what ``Solver`` / ``PeriodicSolver`` return for it alone, except
+that a volume paused for the percolation test skips one tau update. Optional FP64 defect
+correction (``refine=True``) follows per volume.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from timeit import default_timer as timer
+
+import numpy as np
+import torch
+
+from . import _capi
+from ._capi import (TF_BATCH_ACTIVE, TF_BATCH_CONVERGED, TF_BATCH_NEEDS_HOST, TF_KIND_BINARY, TF_PERIODIC_Y,
+                    TF_PERIODIC_Z, TfBatchState, TfGeom, TfOperator, check)
+from .percolation import spans_x
+from .solvers import layer_metrics, refine_field
+
+INTERVAL = 100  # half-sweeps between convergence checks (taufactor.py:184-185)
+
+
+def _ptr(t: torch.Tensor) -> int:
+    return t.data_ptr()
+
+
+class VolumeResult:
+    """Outcome for one volume, with the attributes of the reference solver it stands for."""
+
+    top_bc, bot_bc = -0.5, 0.5
+
+    def __init__(self, img: np.ndarray, periodic: bool):
+        self.cpu_img = img[None]
+        self.batch_size, self.Nx, self.Ny, self.Nz = self.cpu_img.shape
+        self.periodic = periodic
+        self.conductive_labels = [1]
+        mask = self.cpu_img == 1
+        self.vol_x = mask.mean(axis=(2, 3), dtype=np.float64)
+        self.D_mean = np.mean(self.vol_x, axis=1)
+        self.D_0 = 1
+        self.iter = 0
+        self.converged = False
+        self.tau = self.D_eff = self.tau_x = self.c_x = self.flux_1d = None
+        self.residual_history = None
+
+
+class BatchSolve:
+    """Solve binary volumes of any shapes together.
+
+    volumes   sequence of 3-D uint8/bool/int arrays with labels in {0, 1} (1 = conductive)
+    periodic  bool or one bool per volume: PeriodicSolver (periodic y, z) instead of Solver
+    omega     None (each volume's reference default 2 - pi/(1.5 Nx)), a float, or one per volume
+    """
+
+    def __init__(self, volumes, periodic=False, omega=None, device="cuda"):
+        self.device = torch.device(device)
+        if self.device.type != "cuda" or not torch.cuda.is_available():
+            raise RuntimeError("BatchSolve runs on CUDA devices only")
+        if self.device.index is None:
+            self.device = torch.device("cuda", torch.cuda.current_device())
+        vols = [np.asarray(v) for v in volumes]
+        n = len(vols)
+        if n == 0:
+            raise ValueError("no volumes")
+        per = list(periodic) if isinstance(periodic, (list, tuple, np.ndarray)) else [bool(periodic)] * n
+        om = list(omega) if isinstance(omega, (list, tuple, np.ndarray)) else [omega] * n
+        if len(per) != n or len(om) != n:
+            raise ValueError("periodic / omega must give one entry per volume")
+        self.lib = lib = _capi.load()
+        self.n = n
+        self.results = []
+        self.geoms = (TfGeom * n)()
+        self.ops = (TfOperator * n)()
+        self.fa, self.fb, self.codes = [], [], []
+        ty, tz, kk = C.c_int(), C.c_int(), C.c_int()
+        lib.tf_batch_tile(C.byref(ty), C.byref(tz), C.byref(kk))
+        self.k = kk.value
+        work, planes = [], []
+        flux_off, csum_off, d_mean = [], [], []
+        nf = nc = 0
+        with torch.cuda.device(self.device):
+            self.err = torch.zeros(1, dtype=torch.int32, device=self.device)
+            for v, img in enumerate(vols):
+                if img.ndim != 3:
+                    raise ValueError("every volume must be 3-D")
+                u = np.unique(img)
+                if len(u) > 2 or u.max() not in (0, 1) or u.min() not in (0, 1):
+                    raise ValueError(f"volume {v}: labels must be 0/1, got {u}")
+                res = VolumeResult(img, per[v])
+                self.results.append(res)
+                nx, ny, nz = img.shape
+                pflag = (TF_PERIODIC_Y | TF_PERIODIC_Z) if per[v] else 0
+                g = self.geoms[v]
+                check(lib.tf_geometry(1, nx, ny, nz, pflag, C.byref(g)), "tf_geometry")
+                if not g.tiled:
+                    raise _capi.TfError(_capi.TF_ERR_UNSUPPORTED,
+                                        f"BatchSolve volume {v} {img.shape}: periodic faces must be even and >= 16")
+                op = self.ops[v]
+                op.kind = TF_KIND_BINARY
+                op.periodic = pflag
+                w = om[v] if om[v] is not None else 2 - math.pi / (1.5 * nx)
+                op.omega = float(np.float32(w))
+                op.ghost_lo, op.ghost_hi = 2 * res.top_bc, 2 * res.bot_bc
+                op.ky = op.kz = 1.0
+                for i in range(256):
+                    op.divisor[i] = float(i) if 1 <= i <= 8 else np.inf
+                code = torch.empty(g.code_bytes, dtype=torch.uint8, device=self.device)
+                fa = torch.empty(g.field_elems, dtype=torch.float32, device=self.device)
+                fb = torch.zeros(g.field_elems, dtype=torch.float32, device=self.device)
+                sh = 1 / (2 * nx)
+                prof = torch.linspace(res.top_bc + sh, res.bot_bc - sh, nx, dtype=torch.float32).to(self.device)
+                phase = torch.from_numpy(np.ascontiguousarray(img == 1, dtype=np.uint8)).to(self.device)
+                check(lib.tf_pack(C.byref(g), C.byref(op), _ptr(phase), _ptr(prof), _ptr(code), _ptr(fa),
+                                  self._stream()), "tf_pack")
+                self.fa.append(fa)
+                self.fb.append(fb)
+                self.codes.append(code)
+                tiles = ((ny + ty.value - 1) // ty.value) * ((nz + tz.value - 1) // tz.value)
+                work += [(v, t) for t in range(tiles)]
+                planes += [(v, x) for x in range(nx)]
+                flux_off.append(nf)
+                csum_off.append(nc)
+                nf += max(nx - 1, 1)
+                nc += nx
+                d_mean.append(float(res.D_mean[0]))
+            self.work = torch.tensor(work, dtype=torch.int32, device=self.device).reshape(-1)
+            self.planes = torch.tensor(planes, dtype=torch.int32, device=self.device).reshape(-1)
+            self.n_work, self.n_planes = len(work), len(planes)
+            self.flux = torch.zeros(nf, dtype=torch.float64, device=self.device)
+            self.csum = torch.zeros(nc, dtype=torch.float64, device=self.device)
+            self.flux_off, self.csum_off = flux_off, csum_off
+            self.desc = torch.empty(int(lib.tf_batch_desc_bytes(n)), dtype=torch.uint8, device=self.device)
+            P = C.c_void_p * n
+            check(lib.tf_batch_describe(n, self.geoms, self.ops, P(*[_ptr(t) for t in self.fa]),
+                                        P(*[_ptr(t) for t in self.fb]), P(*[_ptr(t) for t in self.codes]),
+                                        (C.c_int64 * n)(*flux_off), (C.c_int64 * n)(*csum_off),
+                                        (C.c_double * n)(*d_mean), _ptr(self.err), _ptr(self.desc)), "tf_batch_describe")
+            i32 = dict(dtype=torch.int32, device=self.device)
+            f64 = dict(dtype=torch.float64, device=self.device)
+            self.status = torch.zeros(n, **i32)
+            self.perc = torch.zeros(n, **i32)
+            self.conv_iter = torch.zeros(n, **i32)
+            self.conv_parity = torch.zeros(n, **i32)
+            self.old_tau = torch.zeros(n, **f64)
+            self.tau = torch.zeros(n, **f64)
+            self.rel = torch.zeros(n, **f64)
+            self.d_rel = torch.zeros(n, **f64)
+            self.iter_base = torch.zeros(1, **i32)
+        self.state = TfBatchState(_ptr(self.status), _ptr(self.perc), _ptr(self.conv_iter), _ptr(self.conv_parity),
+                                  _ptr(self.old_tau), _ptr(self.tau), _ptr(self.rel), _ptr(self.d_rel),
+                                  _ptr(self.iter_base))
+        self.iter_offset = np.zeros(n, dtype=np.int64)
+        self._final_in_b = np.zeros(n, dtype=bool)
+        self.graph = None
+        self.walltime = 0.0
+
+    def _stream(self):
+        return torch.cuda.current_stream(self.device).cuda_stream
+
+    # ---------------------------------------------------------------- device steps
+    def _interval(self, interval: int, start_in_b: int, conv_crit: float):
+        """100 half-sweeps of every active volume, then layer sums and the decision."""
+        lib, st = self.lib, self._stream()
+        parity = start_in_b
+        for _ in range(INTERVAL // self.k):
+            check(lib.tf_batch_advance(_ptr(self.desc), _ptr(self.work), self.n_work, _ptr(self.status), parity, st),
+                  "tf_batch_advance")
+            parity ^= 1
+        check(lib.tf_batch_layer_sums(_ptr(self.desc), _ptr(self.planes), self.n_planes, _ptr(self.status), parity,
+                                      _ptr(self.flux), _ptr(self.csum), st), "tf_batch_layer_sums")
+        check(lib.tf_batch_check(_ptr(self.desc), self.n, _ptr(self.flux), self.state, float(conv_crit), interval,
+                                 parity, st), "tf_batch_check")
+        return parity
+
+    def _pair(self, conv_crit: float):
+        """Two intervals (an even number of launches, so the fields return to buffer A)."""
+        p = self._interval(0, 0, conv_crit)
+        p = self._interval(1, p, conv_crit)
+        check(self.lib.tf_batch_tick(_ptr(self.iter_base), 2 * INTERVAL, self._stream()), "tf_batch_tick")
+        assert p == 0
+
+    def _capture(self, conv_crit: float):
+        g = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream(self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        with torch.cuda.stream(side):
+            with torch.cuda.graph(g, stream=side):
+                self._pair(conv_crit)
+        torch.cuda.current_stream(self.device).wait_stream(side)
+        return g
+
+    def _resolve_paused(self, status: np.ndarray, it: int):
+        """Percolation test for volumes paused on a zero layer flux (taufactor.py:318-327)."""
+        conv_iter = self.conv_iter.cpu().numpy()
+        parity = self.conv_parity.cpu().numpy()
+        for v in np.nonzero(status == TF_BATCH_NEEDS_HOST)[0]:
+            res = self.results[v]
+            if spans_x(res.cpu_img[0] == 1):
+                self.perc[v] = 1
+                # resume: the others advanced in lockstep meanwhile; realign the buffer parity
+                # (graphs always start from buffer A) and remember the skipped half-sweeps
+                if parity[v]:
+                    self.fa[v].copy_(self.fb[v])
+                self.iter_offset[v] += it - conv_iter[v]
+                self.status[v] = TF_BATCH_ACTIVE
+            else:
+                print(f"Warning: volume {v} has no percolating path!")
+                self.perc[v] = 2
+                self.status[v] = TF_BATCH_CONVERGED
+
+    # ---------------------------------------------------------------- public
+    def solve(self, iter_limit: int = 10000, conv_crit: float = 1e-2, graph: bool = True, refine=False,
+              poll: int = 2, verbose: bool = False):
+        """Iterate every volume to the reference's convergence rule or iter_limit (rounded down
+        to a multiple of 200); returns the list of VolumeResult.
+
+        poll: graph replays (200 half-sweeps each) between two reads of the status flags.
+        """
+        limit = (iter_limit // (2 * INTERVAL)) * 2 * INTERVAL
+        start = timer()
+        with torch.cuda.device(self.device):
+            if graph and self.graph is None:
+                self.graph = self._capture(conv_crit)
+                self._graph_crit = conv_crit
+            if graph and self._graph_crit != conv_crit:
+                self.graph = self._capture(conv_crit)
+                self._graph_crit = conv_crit
+            it = 0
+            while it < limit:
+                n_rep = min(poll, (limit - it) // (2 * INTERVAL))
+                for _ in range(n_rep):
+                    if graph:
+                        self.graph.replay()
+                    else:
+                        self._pair(conv_crit)
+                it += n_rep * 2 * INTERVAL
+                status = self.status.cpu().numpy()
+                if (status == TF_BATCH_NEEDS_HOST).any():
+                    self._resolve_paused(status, it)
+                    status = self.status.cpu().numpy()
+                if verbose:
+                    print(f"half-sweeps {it}: {int((status == TF_BATCH_ACTIVE).sum())} of {self.n} active")
+                if not (status == TF_BATCH_ACTIVE).any():
+                    break
+            if int(self.err.item()):
+                raise _capi.TfError(int(self.err.item()), "tf_batch_advance (device)")
+            self._collect(it)
+            if refine:
+                self.refine(**(refine if isinstance(refine, dict) else {}))
+        torch.cuda.synchronize(self.device)
+        self.walltime = timer() - start
+        return self.results
+
+    def _collect(self, it: int):
+        status = self.status.cpu().numpy()
+        conv_iter = self.conv_iter.cpu().numpy()
+        parity = self.conv_parity.cpu().numpy()
+        flux = self.flux.cpu().numpy()
+        csum = self.csum.cpu().numpy()
+        for v, res in enumerate(self.results):
+            nx = res.Nx
+            area = float(res.Ny * res.Nz)
+            res.converged = bool(status[v] == TF_BATCH_CONVERGED)
+            res.iter = int(conv_iter[v] - self.iter_offset[v]) if res.converged else int(it - self.iter_offset[v])
+            # the field the metrics were taken from: buffer B if the decision saw it there
+            self._final_in_b[v] = bool(parity[v]) if res.converged else False
+            res.flux_1d = flux[self.flux_off[v]:self.flux_off[v] + nx - 1][None] / area
+            c_x = csum[self.csum_off[v]:self.csum_off[v] + nx][None] / area
+            if self.perc[v].item() == 2:
+                res.flux_1d = np.zeros_like(res.flux_1d)
+            tau, _ = layer_metrics(res, res.flux_1d, c_x)
+            res.tau = np.where(tau == 0, np.inf, tau) if res.converged else tau
+
+    def field(self, v: int) -> torch.Tensor:
+        """Volume v's field in the reference's padded layout [1,Nx+2,Ny+2,Nz+2]."""
+        res = self.results[v]
+        buf = self.fb[v] if self._final_in_b[v] else self.fa[v]
+        out = torch.empty((1, res.Nx + 2, res.Ny + 2, res.Nz + 2), dtype=torch.float32, device=self.device)
+        with torch.cuda.device(self.device):
+            check(self.lib.tf_unpack(C.byref(self.geoms[v]), C.byref(self.ops[v]), _ptr(buf), _ptr(out),
+                                     self._stream()), "tf_unpack")
+        return out
+
+    def refine(self, tol: float = 1e-10, max_outer: int = 12):
+        """FP64 defect correction of every volume's converged field (see SORSolver.refine)."""
+        lib = self.lib
+        for v, res in enumerate(self.results):
+            cur = self.fb[v] if self._final_in_b[v] else self.fa[v]
+            g, op = self.geoms[v], self.ops[v]
+            c64, hist = refine_field(lib, g, op, cur, self.codes[v], self.err, self._stream(), 1, tol, max_outer,
+                                     max(400, 2 * res.iter))
+            flux = torch.empty(max(res.Nx - 1, 1), dtype=torch.float64, device=self.device)
+            csum = torch.empty(res.Nx, dtype=torch.float64, device=self.device)
+            check(lib.tf_layer_sums_f64(C.byref(g), C.byref(op), _ptr(c64), _ptr(self.codes[v]), _ptr(flux),
+                                        _ptr(csum), self._stream()), "tf_layer_sums_f64")
+            area = float(res.Ny * res.Nz)
+            res.flux_1d = flux.cpu().numpy()[None, : res.Nx - 1] / area
+            tau, _ = layer_metrics(res, res.flux_1d, csum.cpu().numpy()[None] / area)
+            res.tau = np.where(tau == 0, np.inf, tau)
+            res.residual_history = hist
+        return self.results

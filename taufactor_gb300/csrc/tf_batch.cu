@@ -1,0 +1,264 @@
+// Batched solve of many volumes of uneven shapes (sm_103a).
+//
+// Every volume keeps its own split-layout buffers and geometry; a descriptor table in device
+// memory holds, per volume, the TMA tensor maps of its two field buffers and its codes, the
+// sweep arguments for both ping-pong directions and the offsets of its layer sums. One
+// k_stream_multi launch advances every still-active volume by K half-sweeps: CTA w takes work
+// item (volume, tile) from a table and runs the same per-tile body as the single-volume
+// kernel; CTAs of volumes whose status is not "active" return at once. k_layer_sums_multi and
+// k_batch_check then evaluate the reference's convergence rule (taufactor.py:109-153,
+// :293-331) per volume on the device and set its status, so a whole check interval -- sweeps,
+// layer sums, decision -- runs without the host and can be captured in a CUDA graph.
+#include <cstring>
+#include <vector>
+
+#include "tf_stream.cuh"
+
+namespace tf {
+
+constexpr int BTY = 16, BTZ = 64, BK = 4;  // tile and fused depth of the batched sweep
+using BShape = StreamShape<BTY, BTZ, BK>;
+
+struct alignas(64) VolDesc {
+    CUtensorMap map_a, map_b, map_c;  // field A, field B, codes
+    SweepArgs ab, ba;                 // A -> B and B -> A
+    const uint8_t* code;
+    int tiles_z, tiles_y;
+    long long flux_off, csum_off;  // offsets into the layer-sum arenas
+    double d_mean;                 // mean conductive fraction (tau = d_mean / D_rel)
+    double inv_area;               // 1 / (ny * nz)
+};
+
+__global__ void __launch_bounds__(BShape::NT, 2)
+    k_stream_multi(const VolDesc* __restrict__ desc, const int2* __restrict__ work,
+                   const int32_t* __restrict__ status, int parity) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int2 item = work[blockIdx.x];
+    const int v = item.x;
+    if (status[v] != TF_BATCH_ACTIVE) return;
+    const VolDesc* d = desc + v;
+    const int tz = item.y % d->tiles_z, ty = item.y / d->tiles_z;
+    const SweepArgs a = parity ? d->ba : d->ab;
+    stream_tile<TF_KIND_BINARY, BTY, BTZ, BK, false>(parity ? &d->map_b : &d->map_a, &d->map_c, a, nullptr,
+                                                     tz * (BTZ / 2), ty * BTY, 0, smem);
+}
+
+__device__ __forceinline__ double warp_sum_b(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// One CTA per (volume, plane): float64 sums of the masked x-flux through face x|x+1 and of the
+// field in plane x (taufactor.py:294-296, :307, :412-419). Binary operators only.
+__global__ void __launch_bounds__(256) k_layer_sums_multi(const VolDesc* __restrict__ desc,
+                                                          const int2* __restrict__ planes,
+                                                          const int32_t* __restrict__ status, int cur_in_b,
+                                                          double* __restrict__ flux, double* __restrict__ csum) {
+    __shared__ double red[2][8];
+    const int2 item = planes[blockIdx.x];
+    const int v = item.x, x = item.y;
+    if (status[v] != TF_BATCH_ACTIVE) return;
+    const VolDesc* d = desc + v;
+    const Geo g = d->ab.g;
+    const float* field = cur_in_b ? d->ab.out : d->ba.out;  // ab.out is buffer B
+    const bool has_flux = x + 1 < g.NX;
+    const int gm = (half_len(g.NZ, 0) + 3) >> 2;
+    const float* f0 = field + (long long)x * g.plane_f;
+    const uint8_t* c0 = d->code + (long long)x * g.plane_c;
+    double fs = 0.0, cs = 0.0;
+    for (int it = threadIdx.x; it < g.NY * 2 * gm; it += blockDim.x) {
+        const int gi = it % gm;
+        const int r = it / gm;
+        const int y = r >> 1, q = r & 1;
+        const int nj = half_len(g.NZ, q);
+        const int j = 4 * gi;
+        if (j >= nj) continue;
+        const long long off = (long long)(y + HY) * g.row_f + q * g.ZH + HJ + j;
+        const long long offc = (long long)(y + HY) * g.row_c + q * g.ZHC + HJ + j;
+        const float4 a = *reinterpret_cast<const float4*>(f0 + off);
+        float4 bb = a;
+        if (has_flux) bb = *reinterpret_cast<const float4*>(f0 + g.plane_f + off);
+        const float av[4] = {a.x, a.y, a.z, a.w};
+        const float bv[4] = {bb.x, bb.y, bb.z, bb.w};
+        const int n = nj - j < 4 ? nj - j : 4;
+        for (int i = 0; i < n; ++i) {
+            cs += (double)av[i];
+            if (has_flux && c0[offc + i] != 0 && c0[g.plane_c + offc + i] != 0)
+                fs += (double)__fsub_rn(bv[i], av[i]);
+        }
+    }
+    fs = warp_sum_b(fs);
+    cs = warp_sum_b(cs);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) {
+        red[0][w] = fs;
+        red[1][w] = cs;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double a = 0.0, c = 0.0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+            a += red[0][i];
+            c += red[1][i];
+        }
+        if (has_flux) flux[d->flux_off + x] = a;
+        csum[d->csum_off + x] = c;
+    }
+}
+
+// One CTA (one warp) per volume: the reference's convergence rule on its layer fluxes.
+//   rel = (max - min) / max of the layer-mean fluxes (NaN if max == 0); D_rel = mean * Nx;
+//   tau = d_mean / D_rel (NaN if D_rel == 0). Converged iff rel < conv_crit and
+//   |tau - old_tau| < 2e-3; otherwise old_tau = tau. A zero layer flux pauses the volume
+//   (status "needs host") until its percolation is known: non-percolating volumes converge
+//   with tau = 0 (reported as inf), percolating ones continue. A NaN mean converges.
+__global__ void k_batch_check(const VolDesc* __restrict__ desc, int n_vol, const double* __restrict__ flux,
+                              tf_batch_state st, double conv_crit, int interval, int cur_in_b) {
+    const int v = blockIdx.x;
+    if (v >= n_vol || st.status[v] != TF_BATCH_ACTIVE) return;
+    const VolDesc* d = desc + v;
+    const int nx = d->ab.g.NX;
+    const int nf = nx - 1;
+    double mx = -INFINITY, mn = INFINITY, sum = 0.0;
+    for (int i = threadIdx.x; i < nf; i += 32) {
+        const double f = flux[d->flux_off + i] * d->inv_area;
+        mx = fmax(mx, f);
+        mn = fmin(mn, f);
+        sum += f;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        mn = fmin(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+        sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    }
+    if (threadIdx.x != 0) return;
+    const double mean = sum / nf;
+    const int iter = *st.iter_base + 100 * (interval + 1);
+    double rel = mx != 0.0 ? (mx - mn) / mx : NAN;
+    double d_rel = mean * nx;
+    double tau = d_rel != 0.0 ? d->d_mean / d_rel : NAN;
+    if (mn == 0.0 || mx == 0.0 || mean == 0.0) {
+        if (st.perc[v] == 0) {  // percolation unknown: let the host decide
+            st.status[v] = TF_BATCH_NEEDS_HOST;
+            st.conv_iter[v] = iter;
+            st.conv_parity[v] = cur_in_b;
+            return;
+        }
+        if (st.perc[v] == 2) {  // no spanning path: converged, tau reported as inf
+            rel = 0.0;
+            d_rel = 0.0;
+            tau = 0.0;
+        }
+    }
+    if (isnan(mean)) rel = 0.0;
+    st.tau[v] = tau;
+    st.rel[v] = rel;
+    st.d_rel[v] = d_rel;
+    if (rel < conv_crit && fabs(tau - st.old_tau[v]) < 2e-3) {
+        st.status[v] = TF_BATCH_CONVERGED;
+        st.conv_iter[v] = iter;
+        st.conv_parity[v] = cur_in_b;
+    } else {
+        st.old_tau[v] = tau;
+    }
+}
+
+__global__ void k_batch_tick(int32_t* iter_base, int step) { *iter_base += step; }
+
+}  // namespace tf
+
+using namespace tf;
+
+extern "C" {
+
+size_t tf_batch_desc_bytes(int n_vol) { return n_vol > 0 ? (size_t)n_vol * sizeof(VolDesc) : 0; }
+
+void tf_batch_tile(int* tile_y, int* tile_z, int* half_sweeps) {
+    if (tile_y) *tile_y = BTY;
+    if (tile_z) *tile_z = BTZ;
+    if (half_sweeps) *half_sweeps = BK;
+}
+
+int tf_batch_describe(int n_vol, const tf_geom* geoms, const tf_operator* ops, float* const* field_a,
+                      float* const* field_b, const uint8_t* const* codes, const int64_t* flux_off,
+                      const int64_t* csum_off, const double* d_mean, int32_t* err_dev, void* desc_dev) {
+    if (n_vol <= 0 || !geoms || !ops || !field_a || !field_b || !codes || !flux_off || !csum_off || !d_mean ||
+        !desc_dev)
+        return TF_ERR_ARG;
+    std::vector<VolDesc> h(n_vol);
+    for (int v = 0; v < n_vol; ++v) {
+        const tf_geom& gg = geoms[v];
+        const tf_operator& op = ops[v];
+        if (gg.batch != 1 || !gg.tiled || op.kind != TF_KIND_BINARY) return TF_ERR_UNSUPPORTED;
+        VolDesc& d = h[v];
+        std::memset(&d, 0, sizeof(VolDesc));
+        const long long planes = (long long)gg.nx;
+        int rc = encode_map_3d(&d.map_a, field_a[v], 4, gg.zh, 2 * gg.yp, planes, (long long)gg.zh * 4,
+                               (long long)gg.zh * 4 * 2 * gg.yp, BShape::WJ, 2 * BShape::ROWS);
+        if (!rc)
+            rc = encode_map_3d(&d.map_b, field_b[v], 4, gg.zh, 2 * gg.yp, planes, (long long)gg.zh * 4,
+                               (long long)gg.zh * 4 * 2 * gg.yp, BShape::WJ, 2 * BShape::ROWS);
+        if (!rc)
+            rc = encode_map_3d(&d.map_c, codes[v], 1, gg.zhc, 2 * gg.yp, planes, gg.zhc,
+                               (long long)gg.zhc * 2 * gg.yp, BShape::WJC, 2 * BShape::ROWS);
+        if (rc) return rc;
+        const Geo g = make_geo(gg);
+        d.ab = make_args(g, op, field_b[v], 0, BK, err_dev);
+        d.ba = make_args(g, op, field_a[v], 0, BK, err_dev);
+        d.code = codes[v];
+        d.tiles_z = (gg.nz + BTZ - 1) / BTZ;
+        d.tiles_y = (gg.ny + BTY - 1) / BTY;
+        d.flux_off = flux_off[v];
+        d.csum_off = csum_off[v];
+        d.d_mean = d_mean[v];
+        d.inv_area = 1.0 / ((double)gg.ny * gg.nz);
+    }
+    // kernel attributes are set here, outside any stream capture
+    if (cudaFuncSetAttribute(k_stream_multi, cudaFuncAttributeMaxDynamicSharedMemorySize, BShape::SMEM) !=
+        cudaSuccess)
+        return TF_ERR_CUDA;
+    return cudaMemcpy(desc_dev, h.data(), sizeof(VolDesc) * n_vol, cudaMemcpyHostToDevice) == cudaSuccess
+               ? TF_OK
+               : TF_ERR_CUDA;
+}
+
+int tf_batch_advance(const void* desc_dev, const int32_t* work_dev, int n_work, const int32_t* status_dev,
+                     int parity, void* stream) {
+    if (!desc_dev || !work_dev || n_work <= 0 || !status_dev) return TF_ERR_ARG;
+    k_stream_multi<<<n_work, BShape::NT, BShape::SMEM, (cudaStream_t)stream>>>(
+        static_cast<const VolDesc*>(desc_dev), reinterpret_cast<const int2*>(work_dev), status_dev, parity & 1);
+    note_launch();
+    return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
+}
+
+int tf_batch_layer_sums(const void* desc_dev, const int32_t* planes_dev, int n_planes, const int32_t* status_dev,
+                        int cur_in_b, double* flux_dev, double* csum_dev, void* stream) {
+    if (!desc_dev || !planes_dev || n_planes <= 0 || !status_dev || !flux_dev || !csum_dev) return TF_ERR_ARG;
+    k_layer_sums_multi<<<n_planes, 256, 0, (cudaStream_t)stream>>>(static_cast<const VolDesc*>(desc_dev),
+                                                                    reinterpret_cast<const int2*>(planes_dev),
+                                                                    status_dev, cur_in_b & 1, flux_dev, csum_dev);
+    note_launch();
+    return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
+}
+
+int tf_batch_check(const void* desc_dev, int n_vol, const double* flux_dev, tf_batch_state state, double conv_crit,
+                   int interval, int cur_in_b, void* stream) {
+    if (!desc_dev || n_vol <= 0 || !flux_dev || !state.status || !state.perc || !state.conv_iter ||
+        !state.conv_parity || !state.old_tau || !state.tau || !state.rel || !state.d_rel || !state.iter_base)
+        return TF_ERR_ARG;
+    k_batch_check<<<n_vol, 32, 0, (cudaStream_t)stream>>>(static_cast<const VolDesc*>(desc_dev), n_vol, flux_dev,
+                                                          state, conv_crit, interval, cur_in_b & 1);
+    note_launch();
+    return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
+}
+
+int tf_batch_tick(int32_t* iter_base_dev, int half_sweeps, void* stream) {
+    if (!iter_base_dev) return TF_ERR_ARG;
+    k_batch_tick<<<1, 1, 0, (cudaStream_t)stream>>>(iter_base_dev, half_sweeps);
+    note_launch();
+    return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
+}
+
+}  // extern "C"

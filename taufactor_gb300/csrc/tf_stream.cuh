@@ -99,16 +99,16 @@ __device__ __forceinline__ void stage_update(float4& self, const float4& xp, con
     st4(Fp + row_me * WJ + jj, self);
 }
 
+// The CTA's work: one tile (j0 = first staged padded j, y0 = first interior row, volume b of
+// the batch described by `a`) for K half-sweeps. `op` may be null for the binary operator.
+// `tmf` / `tmc` are tensor maps of the input field and the codes (kernel parameter or global
+// memory). Shared memory: StreamShape::SMEM bytes at `smem` (128-byte aligned).
 template <int KIND, int TY, int TZ, int K, bool RHS>
-__global__ void __launch_bounds__(StreamShape<TY, TZ, K>::NT, StreamShape<TY, TZ, K>::NT <= 256 ? 2 : 1)
-    k_stream(const __grid_constant__ CUtensorMap tmf, const __grid_constant__ CUtensorMap tmc, const SweepArgs a,
-             const __grid_constant__ tf_operator op) {
+__device__ __forceinline__ void stream_tile(const CUtensorMap* tmf, const CUtensorMap* tmc, const SweepArgs& a,
+                                            const tf_operator* op, int j0, int y0, int b, unsigned char* smem) {
     using S = StreamShape<TY, TZ, K>;
-    constexpr int G = S::G, WJ = S::WJ, WJC = S::WJC, NS = S::NS, D = S::D, R = S::R, NT = S::NT, TJ = S::TJ;
+    constexpr int G = S::G, WJ = S::WJ, WJC = S::WJC, NS = S::NS, D = S::D, R = S::R, NT = S::NT;
     constexpr int ROWS = S::ROWS;
-    // dynamic shared memory: the runtime aligns it to at least 128 bytes (no static shared
-    // variables precede it in this kernel); every pointer below stays in the shared window
-    extern __shared__ __align__(128) unsigned char smem[];
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
     int* s_fail = reinterpret_cast<int*>(smem + 8 * NS);
     float* lut = reinterpret_cast<float*>(smem + 128);
@@ -121,9 +121,6 @@ __global__ void __launch_bounds__(StreamShape<TY, TZ, K>::NT, StreamShape<TY, TZ
     const int ty = tid / G;
     const int gi = tid - ty * G;
     const int jj = 4 * gi;
-    const int j0 = blockIdx.x * TJ;
-    const int y0 = blockIdx.y * TY;
-    const int b = blockIdx.z;
     const int NX = g.NX;
     const int y = y0 - K + ty;  // interior y of this thread's row (may lie in a ghost band)
     const int row0 = 2 * (y0 + HY - K);  // first staged row of the TMA box (padded coordinates)
@@ -137,9 +134,9 @@ __global__ void __launch_bounds__(StreamShape<TY, TZ, K>::NT, StreamShape<TY, TZ
         *s_fail = 0;
     }
     if (KIND == TF_KIND_ANISOTROPIC)
-        for (int i = tid; i < 256; i += NT) lut[i] = op.divisor[i];
+        for (int i = tid; i < 256; i += NT) lut[i] = op->divisor[i];
     if (KIND == TF_KIND_MULTIPHASE)
-        for (int i = tid; i < 32 * 32; i += NT) lut[i] = op.face[i];
+        for (int i = tid; i < 32 * 32; i += NT) lut[i] = op->face[i];
     fill_division_table(tab, tid);
     for (int s = 0; s < NS; ++s) {
         float* f = F0 + s * (S::SLOT / 4);
@@ -153,8 +150,8 @@ __global__ void __launch_bounds__(StreamShape<TY, TZ, K>::NT, StreamShape<TY, TZ
     auto issue = [&](int x) {
         const int s = x % NS;
         mbar_arrive_expect_tx(&bar[s], S::FBYTES + S::CBYTES);
-        tma_load_3d(F0 + s * (S::SLOT / 4), &tmf, &bar[s], j0, row0, b * NX + x);
-        tma_load_3d(C0 + s * S::SLOT, &tmc, &bar[s], j0, row0, b * NX + x);
+        tma_load_3d(F0 + s * (S::SLOT / 4), tmf, &bar[s], j0, row0, b * NX + x);
+        tma_load_3d(C0 + s * S::SLOT, tmc, &bar[s], j0, row0, b * NX + x);
     };
     if (tid == 0)
         for (int x = 0; x < D && x < NX; ++x) issue(x);
@@ -281,6 +278,16 @@ __global__ void __launch_bounds__(StreamShape<TY, TZ, K>::NT, StreamShape<TY, TZ
             }
         }
     }
+}
+
+template <int KIND, int TY, int TZ, int K, bool RHS>
+__global__ void __launch_bounds__(StreamShape<TY, TZ, K>::NT, StreamShape<TY, TZ, K>::NT <= 256 ? 2 : 1)
+    k_stream(const __grid_constant__ CUtensorMap tmf, const __grid_constant__ CUtensorMap tmc, const SweepArgs a,
+             const __grid_constant__ tf_operator op) {
+    // dynamic shared memory: the runtime aligns it to at least 128 bytes (no static shared
+    // variables precede it in this kernel); every pointer below stays in the shared window
+    extern __shared__ __align__(128) unsigned char smem[];
+    stream_tile<KIND, TY, TZ, K, RHS>(&tmf, &tmc, a, &op, blockIdx.x * (TZ / 2), blockIdx.y * TY, blockIdx.z, smem);
 }
 
 // ------------------------------------------------------------------------------ host side

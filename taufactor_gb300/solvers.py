@@ -149,35 +149,10 @@ class SORSolver:
         (D_eff, tau, flux_1d, c_x, tau_x) come from the float64 field and the float32 field holds
         its rounding.
         """
-        g, lib, dev = self._geom, self._lib, self.device
-        gp, st = C.byref(g), None
-        op0 = TfOperator.from_buffer_copy(self._op)
-        op0.ghost_lo = op0.ghost_hi = 0.0
         n_inner = inner_half_sweeps or max(400, 2 * (self.iter or 200))
-        with torch.cuda.device(dev):
-            st = self._stream()
-            c64 = torch.empty(g.field_elems, dtype=torch.float64, device=dev)
-            check(lib.tf_widen_f64(gp, _ptr(self._cur), _ptr(c64), st), "tf_widen_f64")
-            rhs = torch.zeros(g.field_elems, dtype=torch.float32, device=dev)
-            ea = torch.zeros_like(rhs)
-            eb = torch.zeros_like(rhs)
-            r2 = torch.empty((self.batch_size, self.Nx), dtype=torch.float64, device=dev)
-            b2 = torch.empty_like(r2)
-            hist = []
-            for outer in range(max_outer + 1):
-                check(lib.tf_residual_f64(gp, C.byref(self._op), _ptr(c64), _ptr(self._code), _ptr(rhs), _ptr(r2),
-                                          _ptr(b2), st), "tf_residual_f64")
-                bn = torch.sqrt(b2.sum(dim=1)).clamp_min(1e-300)
-                rel = float((torch.sqrt(r2.sum(dim=1)) / bn).max().item())
-                hist.append(rel)
-                if rel < tol or outer == max_outer:
-                    break
-                ea.zero_()
-                in_b = C.c_int(0)
-                check(lib.tf_advance_rhs(gp, C.byref(op0), _ptr(ea), _ptr(eb), _ptr(self._code), _ptr(rhs), 0,
-                                         n_inner, _ptr(self._err), C.byref(in_b), st), "tf_advance_rhs")
-                check(lib.tf_axpy_f64(gp, _ptr(c64), _ptr(eb if in_b.value else ea), st), "tf_axpy_f64")
-            check(lib.tf_narrow_f64(gp, C.byref(self._op), _ptr(c64), _ptr(self._cur), st), "tf_narrow_f64")
+        with torch.cuda.device(self.device):
+            c64, hist = refine_field(self._lib, self._geom, self._op, self._cur, self._code, self._err,
+                                     self._stream(), self.batch_size, tol, max_outer, n_inner)
         self._field64 = c64
         self.residual_history = hist
         self.tau, _ = self.compute_metrics()
@@ -352,6 +327,39 @@ class SORSolver:
                   f"{torch.cuda.max_memory_reserved(device=self.device) / 1e6:.2f} MB reserved)")
 
 
+def refine_field(lib, g: TfGeom, op: TfOperator, cur: torch.Tensor, code: torch.Tensor, err: torch.Tensor, stream,
+                 batch: int, tol: float, max_outer: int, n_inner: int):
+    """FP64 defect correction of the float32 field `cur` (updated in place with the rounding of
+    the result); returns the float64 field and the max-over-volumes relative residual history."""
+    gp = C.byref(g)
+    op0 = TfOperator.from_buffer_copy(op)
+    op0.ghost_lo = op0.ghost_hi = 0.0
+    dev = cur.device
+    c64 = torch.empty(g.field_elems, dtype=torch.float64, device=dev)
+    check(lib.tf_widen_f64(gp, _ptr(cur), _ptr(c64), stream), "tf_widen_f64")
+    rhs = torch.zeros(g.field_elems, dtype=torch.float32, device=dev)
+    ea = torch.zeros_like(rhs)
+    eb = torch.zeros_like(rhs)
+    r2 = torch.empty((batch, g.nx), dtype=torch.float64, device=dev)
+    b2 = torch.empty_like(r2)
+    hist = []
+    for outer in range(max_outer + 1):
+        check(lib.tf_residual_f64(gp, C.byref(op), _ptr(c64), _ptr(code), _ptr(rhs), _ptr(r2), _ptr(b2), stream),
+              "tf_residual_f64")
+        bn = torch.sqrt(b2.sum(dim=1)).clamp_min(1e-300)
+        rel = float((torch.sqrt(r2.sum(dim=1)) / bn).max().item())
+        hist.append(rel)
+        if rel < tol or outer == max_outer:
+            break
+        ea.zero_()
+        in_b = C.c_int(0)
+        check(lib.tf_advance_rhs(gp, C.byref(op0), _ptr(ea), _ptr(eb), _ptr(code), _ptr(rhs), 0, n_inner, _ptr(err),
+                                 C.byref(in_b), stream), "tf_advance_rhs")
+        check(lib.tf_axpy_f64(gp, _ptr(c64), _ptr(eb if in_b.value else ea), stream), "tf_axpy_f64")
+    check(lib.tf_narrow_f64(gp, C.byref(op), _ptr(c64), _ptr(cur), stream), "tf_narrow_f64")
+    return c64, hist
+
+
 class ThroughTransportSolver(SORSolver):
     """Dirichlet x-faces at (-0.5, 0.5), flux-based metrics (taufactor.py:272-331)."""
 
@@ -362,31 +370,39 @@ class ThroughTransportSolver(SORSolver):
     def compute_metrics(self):
         """taufactor.py:293-331 on float64 layer means read back from the device."""
         self.flux_1d, c_x = self._layer_means()
-        fl_max = np.max(self.flux_1d, axis=1)
-        fl_min = np.min(self.flux_1d, axis=1)
-        mean_fl = np.mean(self.flux_1d, axis=1)
-        relative_error = np.divide(fl_max - fl_min, fl_max, out=np.full_like(fl_max, np.nan), where=fl_max != 0)
-        D_rel = mean_fl * self.Nx / abs(self.top_bc - self.bot_bc)
-        tau = np.divide(self.D_mean, D_rel, out=np.full_like(D_rel, np.nan), where=D_rel != 0)
-        c_x = np.divide(c_x, self.vol_x, out=np.zeros_like(self.vol_x), where=self.vol_x != 0)
-        self.c_x = c_x
-        flux_from_c = c_x[:, 1:] - c_x[:, :-1]
-        flux_from_c[self.vol_x[:, 1:] == 0] = 0
-        flux_from_c[self.vol_x[:, :-1] == 0] = 0
-        eps = 0.5 * (self.vol_x[:, :-1] + self.vol_x[:, 1:])
-        self.tau_x = np.divide(eps * flux_from_c, self.flux_1d, out=np.full_like(flux_from_c, np.nan),
-                               where=self.flux_1d != 0)
-        for b in range(self.batch_size):
-            if (fl_min[b] == 0) or (fl_max[b] == 0) or (mean_fl[b] == 0):
-                if not spans_x(np.isin(self.cpu_img[b], self.conductive_labels)):
-                    print(f"Warning: batch element {b} has no percolating path!")
-                    relative_error[b] = 0
-                    D_rel[b] = 0
-                    tau[b] = 0
-                    self.tau_x[b, :] = 0
-        relative_error[np.isnan(mean_fl)] = 0
-        self.D_eff = self.D_0 * D_rel
-        return tau, relative_error
+        return layer_metrics(self, self.flux_1d, c_x)
+
+
+def layer_metrics(s, flux_1d: np.ndarray, c_x_raw: np.ndarray):
+    """The reference's metric arithmetic on per-layer means (taufactor.py:297-331).
+
+    ``s`` provides Nx, top_bc, bot_bc, D_mean, D_0, vol_x [B,Nx], batch_size, cpu_img and
+    conductive_labels; it receives c_x, tau_x and D_eff. Returns (tau, relative_error).
+    """
+    fl_max = np.max(flux_1d, axis=1)
+    fl_min = np.min(flux_1d, axis=1)
+    mean_fl = np.mean(flux_1d, axis=1)
+    relative_error = np.divide(fl_max - fl_min, fl_max, out=np.full_like(fl_max, np.nan), where=fl_max != 0)
+    D_rel = mean_fl * s.Nx / abs(s.top_bc - s.bot_bc)
+    tau = np.divide(s.D_mean, D_rel, out=np.full_like(D_rel, np.nan), where=D_rel != 0)
+    c_x = np.divide(c_x_raw, s.vol_x, out=np.zeros_like(s.vol_x), where=s.vol_x != 0)
+    s.c_x = c_x
+    flux_from_c = c_x[:, 1:] - c_x[:, :-1]
+    flux_from_c[s.vol_x[:, 1:] == 0] = 0
+    flux_from_c[s.vol_x[:, :-1] == 0] = 0
+    eps = 0.5 * (s.vol_x[:, :-1] + s.vol_x[:, 1:])
+    s.tau_x = np.divide(eps * flux_from_c, flux_1d, out=np.full_like(flux_from_c, np.nan), where=flux_1d != 0)
+    for b in range(s.batch_size):
+        if (fl_min[b] == 0) or (fl_max[b] == 0) or (mean_fl[b] == 0):
+            if not spans_x(np.isin(s.cpu_img[b], s.conductive_labels)):
+                print(f"Warning: batch element {b} has no percolating path!")
+                relative_error[b] = 0
+                D_rel[b] = 0
+                tau[b] = 0
+                s.tau_x[b, :] = 0
+    relative_error[np.isnan(mean_fl)] = 0
+    s.D_eff = s.D_0 * D_rel
+    return tau, relative_error
 
 
 class Solver(ThroughTransportSolver):
