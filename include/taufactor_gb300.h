@@ -224,6 +224,21 @@ int tf_batch_check(const void* desc_dev, int n_vol, const double* flux_dev, tf_b
 /* *iter_base_dev += half_sweeps (stream-ordered). */
 int tf_batch_tick(int32_t* iter_base_dev, int half_sweeps, void* stream);
 
+/* tf_batch_layer_sums followed by tf_batch_check, for callers that cannot give the library any
+ * device memory beyond their own buffers (a host whose GPU memory another framework has
+ * reserved in full, or a binding that never links the CUDA allocator). The per-plane sums go to
+ * a static array inside the library instead of caller arenas; only `state` is written, so the
+ * per-layer sums themselves are not returned. No counterpart in the reference.
+ *   Limit: flux_len and csum_len (the arena lengths the descriptor's offsets were built for:
+ *   sum of nx-1, resp. nx, over the volumes) must each be <= 65536, else TF_ERR_UNSUPPORTED.
+ *   Allocates nothing (no cudaMalloc/cudaFree). The first call on a device looks up the device
+ *   address of the static array for that device (make it before any stream capture); the
+ *   array is shared by every call in the process and keeps the last call's contents, so calls
+ *   whose work overlaps on the GPU race. It holds 1 MiB on every GPU that loads the library. */
+int tf_batch_converge_static(const void* desc_dev, const int32_t* planes_dev, int n_planes, int n_vol,
+                             int64_t flux_len, int64_t csum_len, tf_batch_state state, double conv_crit,
+                             int interval, int cur_in_b, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

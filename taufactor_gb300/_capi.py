@@ -22,6 +22,7 @@ EXPORTS = (
     "tf_layer_sums", "tf_unpack", "tf_repack", "tf_check_small_division", "tf_advance_rhs", "tf_widen_f64",
     "tf_narrow_f64", "tf_axpy_f64", "tf_residual_f64", "tf_layer_sums_f64", "tf_batch_desc_bytes", "tf_batch_tile",
     "tf_batch_describe", "tf_batch_advance", "tf_batch_layer_sums", "tf_batch_check", "tf_batch_tick",
+    "tf_batch_converge_static",
 )
 TF_BATCH_ACTIVE, TF_BATCH_CONVERGED, TF_BATCH_NEEDS_HOST = 0, 1, 2
 
@@ -97,6 +98,7 @@ def load():
         "tf_batch_layer_sums": (i32, [vp, vp, i32, vp, i32, vp, vp, vp]),
         "tf_batch_check": (i32, [vp, i32, vp, TfBatchState, C.c_double, i32, i32, vp]),
         "tf_batch_tick": (i32, [vp, i32, vp]),
+        "tf_batch_converge_static": (i32, [vp, vp, i32, i32, i64, i64, TfBatchState, C.c_double, i32, i32, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

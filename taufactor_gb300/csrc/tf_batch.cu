@@ -10,6 +10,7 @@
 // :293-331) per volume on the device and set its status, so a whole check interval -- sweeps,
 // layer sums, decision -- runs without the host and can be captured in a CUDA graph.
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "tf_stream.cuh"
@@ -262,3 +263,63 @@ int tf_batch_tick(int32_t* iter_base_dev, int half_sweeps, void* stream) {
 }
 
 }  // extern "C"
+
+// ------------------------------------------------------------------------------ allocation-free
+// check step. Some callers cannot hand the library any device memory beyond their own inputs
+// and outputs: a host whose device memory is fully reserved up front by another framework's
+// pool, or a language binding that never links the CUDA allocator and only passes buffers it
+// already owns. For them, tf_batch_converge_static runs the batched convergence step (the
+// per-plane layer sums that tf_batch_layer_sums writes into caller arenas, then the decision of
+// tf_batch_check) with the per-plane sums kept in this library's own statically sized device
+// array. The array lives in every GPU that loads the library until the process exits.
+namespace tf {
+
+constexpr long long STATIC_PLANES = 1 << 16;  // capacity of each half of the static scratch
+
+// [0, STATIC_PLANES): per-plane flux sums; [STATIC_PLANES, 2*STATIC_PLANES): field sums.
+static __device__ __align__(256) double g_static_sums[2 * STATIC_PLANES];
+
+// Device address of g_static_sums per device, resolved once with that device current.
+static double* static_sums_address() {
+    constexpr int MAX_DEVICES = 64;
+    static double* addr[MAX_DEVICES] = {nullptr};
+    static std::mutex mu;
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return nullptr;
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_static_sums) != cudaSuccess) return nullptr;
+        addr[dev] = static_cast<double*>(p);
+    }
+    return addr[dev];
+}
+
+}  // namespace tf
+
+extern "C" int tf_batch_converge_static(const void* desc_dev, const int32_t* planes_dev, int n_planes, int n_vol,
+                                        int64_t flux_len, int64_t csum_len, tf_batch_state state,
+                                        double conv_crit, int interval, int cur_in_b, void* stream) {
+    if (!desc_dev || !planes_dev || n_planes <= 0 || n_vol <= 0 || !state.status || !state.perc ||
+        !state.conv_iter || !state.conv_parity || !state.old_tau || !state.tau || !state.rel || !state.d_rel ||
+        !state.iter_base)
+        return TF_ERR_ARG;
+    // the descriptor's layer-sum offsets must fit the static array: flux_len / csum_len are the
+    // arena lengths the descriptor was built for (sum of nx-1, resp. nx, over the volumes)
+    if (flux_len <= 0 || csum_len <= 0 || flux_len > STATIC_PLANES || csum_len > STATIC_PLANES)
+        return TF_ERR_UNSUPPORTED;
+    double* sums = static_sums_address();
+    if (!sums) return TF_ERR_CUDA;
+    cudaStream_t st = (cudaStream_t)stream;
+    // every sum the decision reads is written by the layer-sum launch of this same call, so
+    // nothing in the shared array has to start at zero
+    k_layer_sums_multi<<<n_planes, 256, 0, st>>>(static_cast<const VolDesc*>(desc_dev),
+                                                  reinterpret_cast<const int2*>(planes_dev), state.status,
+                                                  cur_in_b & 1, sums, sums + STATIC_PLANES);
+    note_launch();
+    if (cudaGetLastError() != cudaSuccess) return TF_ERR_CUDA;
+    k_batch_check<<<n_vol, 32, 0, st>>>(static_cast<const VolDesc*>(desc_dev), n_vol, sums, state, conv_crit,
+                                        interval, cur_in_b & 1);
+    note_launch();
+    return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
+}
