@@ -33,6 +33,10 @@ UNIT = "voxel-updates/s"
 N_VOL, SIDE, SIGMA = 16, 256, 2.0
 CONV_CRIT = 1e-4
 CPU_SAMPLE_HALF_SWEEPS = 10
+# DRAM bytes per voxel moved by one launch of the fused sweep (16x128 tile, 4 half-sweeps):
+# dram__bytes_read.sum + dram__bytes_write.sum from one ncu capture on 4 x 256^3 blurred-noise
+# volumes (645 MB for 67.1 M voxels); traffic grows in proportion to the voxels processed.
+TRAFFIC_BYTES_PER_VOXEL_LAUNCH = 645.2e6 / (4 * 256 ** 3)
 
 
 def workload_config(extra=None):
@@ -230,6 +234,8 @@ def run_ours(args):
     s.event_log = None
     peak, peak_kind = measured_peak_hbm()
     achieved = adv_half * V / 2 * 8 / (adv_ms / 1e3) / 1e9  # GB/s of algorithmic bytes (8 B per update)
+    algo_gb_launch = kmax * V / 2 * 8 / 1e9
+    traffic_gb_launch = TRAFFIC_BYTES_PER_VOXEL_LAUNCH * V / 1e9 if (kmax == 4 and s._op.tile == 1) else None
     dram_min = n_tiled * V * 8 / (adv_ms / 1e3) / 1e9  # read + write of the field once per launch
     # accuracy: the timed result against the FP64 solution of the same operator (float64 defect
     # correction on the device to a relative residual of 1e-10)
@@ -273,7 +279,8 @@ def run_ours(args):
                      "fp64_reference": "float64 defect correction of the same operator on the device"},
         "kernel_config": {"tile": int(s._op.tile), "half_sweeps_per_launch": int(kmax), "autotune_ms_per_half_sweep": tuning},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "peak_source": peak_kind, "traffic": None,
+                     "peak_source": peak_kind, "traffic": traffic_gb_launch, "traffic_unit": "GB per launch (ncu)",
+                     "algorithmic_GB_per_launch": algo_gb_launch,
                      "per_unit": "8 B per voxel-update (read + write of float32 c)",
                      "dram_min_GBps": dram_min, "kernel": f"k_stream ({kmax} half-sweeps per launch)",
                      "avg_launch_ms": adv_ms / max(n_tiled, 1)},

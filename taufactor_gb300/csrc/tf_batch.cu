@@ -13,6 +13,7 @@
 #include <mutex>
 #include <vector>
 
+#include "tf_layers.cuh"
 #include "tf_stream.cuh"
 
 namespace tf {
@@ -44,19 +45,13 @@ __global__ void __launch_bounds__(BShape::NT, 2)
                                                      tz * (BTZ / 2), ty * BTY, 0, smem);
 }
 
-__device__ __forceinline__ double warp_sum_b(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
 // One CTA per (volume, plane): float64 sums of the masked x-flux through face x|x+1 and of the
-// field in plane x (taufactor.py:294-296, :307, :412-419). Binary operators only.
+// field in plane x (taufactor.py:294-296, :307, :412-419), exactly as the single-volume
+// k_layer_sums sums them. Binary operators only.
 __global__ void __launch_bounds__(256) k_layer_sums_multi(const VolDesc* __restrict__ desc,
                                                           const int2* __restrict__ planes,
                                                           const int32_t* __restrict__ status, int cur_in_b,
                                                           double* __restrict__ flux, double* __restrict__ csum) {
-    __shared__ double red[2][8];
     const int2 item = planes[blockIdx.x];
     const int v = item.x, x = item.y;
     if (status[v] != TF_BATCH_ACTIVE) return;
@@ -64,47 +59,13 @@ __global__ void __launch_bounds__(256) k_layer_sums_multi(const VolDesc* __restr
     const Geo g = d->ab.g;
     const float* field = cur_in_b ? d->ab.out : d->ba.out;  // ab.out is buffer B
     const bool has_flux = x + 1 < g.NX;
-    const int gm = (half_len(g.NZ, 0) + 3) >> 2;
-    const float* f0 = field + (long long)x * g.plane_f;
-    const uint8_t* c0 = d->code + (long long)x * g.plane_c;
     double fs = 0.0, cs = 0.0;
-    for (int it = threadIdx.x; it < g.NY * 2 * gm; it += blockDim.x) {
-        const int gi = it % gm;
-        const int r = it / gm;
-        const int y = r >> 1, q = r & 1;
-        const int nj = half_len(g.NZ, q);
-        const int j = 4 * gi;
-        if (j >= nj) continue;
-        const long long off = (long long)(y + HY) * g.row_f + q * g.ZH + HJ + j;
-        const long long offc = (long long)(y + HY) * g.row_c + q * g.ZHC + HJ + j;
-        const float4 a = *reinterpret_cast<const float4*>(f0 + off);
-        float4 bb = a;
-        if (has_flux) bb = *reinterpret_cast<const float4*>(f0 + g.plane_f + off);
-        const float av[4] = {a.x, a.y, a.z, a.w};
-        const float bv[4] = {bb.x, bb.y, bb.z, bb.w};
-        const int n = nj - j < 4 ? nj - j : 4;
-        for (int i = 0; i < n; ++i) {
-            cs += (double)av[i];
-            if (has_flux && c0[offc + i] != 0 && c0[g.plane_c + offc + i] != 0)
-                fs += (double)__fsub_rn(bv[i], av[i]);
-        }
-    }
-    fs = warp_sum_b(fs);
-    cs = warp_sum_b(cs);
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    if (l == 0) {
-        red[0][w] = fs;
-        red[1][w] = cs;
-    }
-    __syncthreads();
+    plane_partials<TF_KIND_BINARY>(field + (long long)x * g.plane_f, d->code + (long long)x * g.plane_c, g, has_flux,
+                                   nullptr, fs, cs);
+    block_sum_pair(fs, cs);
     if (threadIdx.x == 0) {
-        double a = 0.0, c = 0.0;
-        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
-            a += red[0][i];
-            c += red[1][i];
-        }
-        if (has_flux) flux[d->flux_off + x] = a;
-        csum[d->csum_off + x] = c;
+        if (has_flux) flux[d->flux_off + x] = fs;
+        csum[d->csum_off + x] = cs;
     }
 }
 

@@ -11,6 +11,7 @@
 //               so the result does not depend on scheduling.
 #include "tf_common.cuh"
 #include "tf_internal.h"
+#include "tf_layers.cuh"
 
 namespace tf {
 
@@ -114,75 +115,25 @@ __global__ void k_repack(const float* __restrict__ padded, float* __restrict__ f
     field[((long long)bx * g.YP + Y) * 2 * g.ZH + pos] = v;
 }
 
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
 template <int KIND>
 __global__ void __launch_bounds__(256) k_layer_sums(const float* __restrict__ field, const uint8_t* __restrict__ code,
                                                     double* __restrict__ flux, double* __restrict__ csum,
                                                     const Geo g, const __grid_constant__ tf_operator op) {
     __shared__ float lut[32 * 32];
-    __shared__ double red[2][8];
-    if (KIND == TF_KIND_MULTIPHASE) {
+    if (KIND == TF_KIND_MULTIPHASE)
         for (int i = threadIdx.x; i < 32 * 32; i += blockDim.x) lut[i] = op.face[i];
-    } else {
+    if (KIND == TF_KIND_ANISOTROPIC)
         for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = op.divisor[i];
-    }
     __syncthreads();
     const int x = blockIdx.x, b = blockIdx.y;
     const bool has_flux = x + 1 < g.NX;
-    const int gm = (half_len(g.NZ, 0) + 3) >> 2;
-    const float* f0 = field + (long long)b * g.vol_f + (long long)x * g.plane_f;
-    const uint8_t* c0 = code + (long long)b * g.vol_c + (long long)x * g.plane_c;
     double fs = 0.0, cs = 0.0;
-    for (int it = threadIdx.x; it < g.NY * 2 * gm; it += blockDim.x) {
-        const int gi = it % gm;
-        const int r = it / gm;
-        const int y = r >> 1, q = r & 1;
-        const int nj = half_len(g.NZ, q);
-        const int j = 4 * gi;
-        if (j >= nj) continue;
-        const long long off = (long long)(y + HY) * g.row_f + q * g.ZH + HJ + j;
-        const long long offc = (long long)(y + HY) * g.row_c + q * g.ZHC + HJ + j;
-        const float4 a = *reinterpret_cast<const float4*>(f0 + off);
-        float4 bb = a;
-        if (has_flux) bb = *reinterpret_cast<const float4*>(f0 + g.plane_f + off);
-        const float av[4] = {a.x, a.y, a.z, a.w};
-        const float bv[4] = {bb.x, bb.y, bb.z, bb.w};
-        const int n = nj - j < 4 ? nj - j : 4;
-        for (int i = 0; i < n; ++i) {
-            cs += (double)av[i];
-            if (has_flux) {
-                const float d = __fsub_rn(bv[i], av[i]);
-                const int ca = c0[offc + i], cb = c0[g.plane_c + offc + i];
-                if (KIND == TF_KIND_MULTIPHASE) {
-                    fs += (double)__fmul_rn(lut[ca * 32 + cb], d);
-                } else if (lut[ca] <= 8.0f && lut[cb] <= 8.0f) {
-                    // Solver.vertical_flux zeroes faces where either factor exceeds 8 (:417-418)
-                    fs += (double)d;
-                }
-            }
-        }
-    }
-    fs = warp_sum(fs);
-    cs = warp_sum(cs);
-    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-    if (l == 0) {
-        red[0][w] = fs;
-        red[1][w] = cs;
-    }
-    __syncthreads();
+    plane_partials<KIND>(field + (long long)b * g.vol_f + (long long)x * g.plane_f,
+                         code + (long long)b * g.vol_c + (long long)x * g.plane_c, g, has_flux, lut, fs, cs);
+    block_sum_pair(fs, cs);
     if (threadIdx.x == 0) {
-        double a = 0.0, c = 0.0;
-        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
-            a += red[0][i];
-            c += red[1][i];
-        }
-        if (has_flux) flux[(long long)b * (g.NX - 1) + x] = a;
-        csum[(long long)b * g.NX + x] = c;
+        if (has_flux) flux[(long long)b * (g.NX - 1) + x] = fs;
+        csum[(long long)b * g.NX + x] = cs;
     }
 }
 
@@ -224,6 +175,8 @@ int layer_sums(const tf_geom& gg, const tf_operator& op, const float* field, con
     dim3 grid(gg.nx, gg.batch);
     if (op.kind == TF_KIND_MULTIPHASE)
         k_layer_sums<TF_KIND_MULTIPHASE><<<grid, 256, 0, st>>>(field, code, flux, csum, g, op);
+    else if (op.kind == TF_KIND_ANISOTROPIC)
+        k_layer_sums<TF_KIND_ANISOTROPIC><<<grid, 256, 0, st>>>(field, code, flux, csum, g, op);
     else
         k_layer_sums<TF_KIND_BINARY><<<grid, 256, 0, st>>>(field, code, flux, csum, g, op);
     note_launch();
