@@ -40,6 +40,22 @@ def _ptr(t: torch.Tensor) -> int:
     return t.data_ptr()
 
 
+def unique_labels(img: np.ndarray) -> np.ndarray:
+    """np.unique(img), with a fast path for integer/bool images spanning at most 64 values."""
+    a = np.asarray(img)
+    if a.size and (a.dtype == bool or a.dtype.kind in "iu"):
+        lo, hi = int(a.min()), int(a.max())
+        if hi - lo < 64:
+            return np.array([v for v in range(lo, hi + 1) if v in (lo, hi) or (a == v).any()], dtype=a.dtype)
+    return np.unique(a)
+
+
+def plane_fraction(mask: np.ndarray) -> np.ndarray:
+    """Mean of a bool [B,X,Y,Z] mask over (Y, Z) in float64, [B,X] (taufactor.py:42)."""
+    B, X = mask.shape[:2]
+    return np.count_nonzero(mask.reshape(B, X, -1), axis=2) / float(np.prod(mask.shape[2:]))
+
+
 class SORSolver:
     """Template of the red-black SOR solve (taufactor.py:15-269).
 
@@ -63,7 +79,7 @@ class SORSolver:
             omega = 2 - math.pi / (1.5 * self.Nx)  # taufactor.py:36-37
         self.omega = omega
         phase, mask = self._phase_indices()
-        self.vol_x = mask.mean(axis=(2, 3), dtype=np.float64)
+        self.vol_x = plane_fraction(mask)
         self._op = self._operator(float(omega))
         autotune.apply(self, *autotune.default_config(self))
         self._build(phase)
@@ -416,9 +432,16 @@ class Solver(ThroughTransportSolver):
         self.D_mean = np.mean(self.vol_x, axis=1)
 
     def _check_binary_labels(self, img):
-        """taufactor.py:387-397 (same message)."""
-        u = np.unique(img)
-        if len(u) > 2 or u.max() not in [0, 1] or u.min() not in [0, 1]:
+        """taufactor.py:387-397 (same message): every label must be 0 or 1."""
+        a = np.asarray(img)
+        if a.dtype == bool:
+            return
+        if a.dtype.kind in "iu":
+            ok = a.size > 0 and a.min() >= 0 and a.max() <= 1
+        else:
+            ok = a.size > 0 and bool(np.logical_or(a == 0, a == 1).all())
+        if not ok:
+            u = np.unique(img)
             raise ValueError(
                 "Input image must only contain 0s and 1s. "
                 "Your image must be segmented to use this tool. "
@@ -519,7 +542,7 @@ class MultiPhaseSolver(ThroughTransportSolver):
             if (not np.isfinite(D_p)) or (D_p < 0):
                 raise ValueError(f"Diffusivity for label {phase} must be finite and >= 0, got {D_p}")
         self.Ds = diffusivities
-        missing_labels = sorted(int(lbl) for lbl in np.unique(img) if lbl not in self.Ds)
+        missing_labels = sorted(int(lbl) for lbl in unique_labels(img) if lbl not in self.Ds)
         if missing_labels:
             warnings.warn("No diffusivity provided for phase label(s) "
                           f"{missing_labels}; assuming these phases are isolating.", UserWarning)
@@ -527,12 +550,12 @@ class MultiPhaseSolver(ThroughTransportSolver):
                 self.Ds[lbl] = 0.0
         self.conductive_labels = [lbl for lbl, D_p in self.Ds.items() if D_p > 0]
         super().__init__(img, omega=omega, device=device)
-        self.VF = {int(p): np.mean(self.cpu_img == p, axis=(1, 2, 3)) for p in np.unique(self.cpu_img)}
+        self.VF = {int(p): np.mean(self.cpu_img == p, axis=(1, 2, 3)) for p in unique_labels(self.cpu_img)}
         self.D_0 = D_scaling
         self.D_mean = np.sum([self.VF[z] * self.Ds.get(z, 0.0) for z in self.VF], axis=0)
 
     def _phase_indices(self):
-        labels = np.unique(self.cpu_img)
+        labels = unique_labels(self.cpu_img)
         if len(labels) > TF_MAX_PHASES:
             raise _capi.TfError(_capi.TF_ERR_UNSUPPORTED,
                                 f"MultiPhaseSolver with {len(labels)} labels (at most {TF_MAX_PHASES})")
