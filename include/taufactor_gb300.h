@@ -239,6 +239,50 @@ int tf_batch_converge_static(const void* desc_dev, const int32_t* planes_dev, in
                              int64_t flux_len, int64_t csum_len, tf_batch_state state, double conv_crit,
                              int interval, int cur_in_b, void* stream);
 
+/* ---------------------------------------------------------------- per-voxel conductivity
+ * MultiPhaseSolver's operator (taufactor.py:508-620) with the diffusivity given per voxel as a
+ * float32 field kappa >= 0 instead of per label, plus its adjoint. With kappa = D[label] the
+ * faces, factor and half-sweeps equal MultiPhaseSolver's bit for bit. kappa_split_dev is a
+ * float [field_elems] buffer in the field layout written by tf_kappa_pack. No reference
+ * counterpart for the adjoint: the reference solve runs under no_grad (taufactor.py:172). */
+
+/* kappa_dev float [batch][nx][ny][nz] -> kappa_split_dev (ghost cells 0 / wrapped copies) and
+ * the initial field (profile[x] where kappa > 0; taufactor.py:282-291, :571-575). */
+int tf_kappa_pack(const tf_geom* g, const tf_operator* op, const float* kappa_dev, const float* profile_dev,
+                  float* kappa_split_dev, float* field_dev, void* stream);
+
+/* n_half half-sweeps in place (taufactor.py:174-182 with :606-613 on per-voxel faces); rhs_dev
+ * (float [field_elems], may be NULL) is added to the neighbour sum for correction solves. */
+int tf_kappa_advance(const tf_geom* g, const tf_operator* op, float* field_dev, const float* kappa_split_dev,
+                     const float* rhs_dev, int first_colour, int n_half, void* stream);
+
+/* per-plane float64 sums of face * (c[x+1] - c[x]) and of c (taufactor.py:615-620, :296, :307);
+ * field_dev is float (field_is_f64 = 0) or double (1). */
+int tf_kappa_layer_sums(const tf_geom* g, const void* field_dev, int field_is_f64, const float* kappa_split_dev,
+                        double* flux_sum_dev, double* c_sum_dev, void* stream);
+
+/* float64 residual r = b - A c; b = the Dirichlet terms of op (b64_dev NULL) or b64_dev
+ * (double [field_elems]). r -> rhs_dev (float, periodic ghosts rebuilt); per-plane sums of r^2
+ * and b^2 -> r2_sum_dev / b2_sum_dev [batch][nx]. */
+int tf_kappa_residual_f64(const tf_geom* g, const tf_operator* op, const double* field64_dev,
+                          const float* kappa_split_dev, const double* b64_dev, float* rhs_dev, double* r2_sum_dev,
+                          double* b2_sum_dev, void* stream);
+
+/* Adjoint right-hand side dD_eff/dc = scale * (face_{x-1|x} - face_{x|x+1}) per voxel
+ * (double [field_elems]); scale = D_0 nx / (|bc_hi - bc_lo| (nx-1) ny nz). */
+int tf_kappa_adjoint_rhs(const tf_geom* g, const float* kappa_split_dev, double* out64_dev, double scale,
+                         void* stream);
+
+/* dD_eff/dkappa per voxel, double [batch][nx][ny][nz], from the float64 field c and the adjoint
+ * lambda (A lambda = dD_eff/dc): interior faces -(lam_u - lam_w)(c_u - c_w) (+ scale *
+ * (c[x+1]-c[x]) on x-faces) times 2 k_w^2/(k_u+k_w)^2, Dirichlet faces 2 lam_u (bc - c_u). */
+int tf_kappa_gradient(const tf_geom* g, const tf_operator* op, const double* field64_dev,
+                      const double* lambda64_dev, const float* kappa_split_dev, double* grad_dev, double scale,
+                      double bc_lo, double bc_hi, void* stream);
+
+/* double field layout -> natural [batch][nx][ny][nz]. */
+int tf_split_to_natural_f64(const tf_geom* g, const double* split_dev, double* natural_dev, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

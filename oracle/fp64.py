@@ -154,3 +154,63 @@ def d_eff_fp64(o: OracleSolve, rtol: float = 1e-10):
     flux = layer_flux_fp64(o, field)
     d_rel = flux.mean(axis=1) * o.Nx / abs(o.top_bc - o.bot_bc)
     return o.D_0 * d_rel, field, resid
+
+
+def adjoint_gradient_fp64(o: OracleSolve, rtol: float = 1e-12):
+    """FP64 dD_eff/dkappa [B,X,Y,Z] of a per-voxel conductivity field (kind 'kappa' /
+    'periodic_kappa'), by the adjoint method on the operator assembled above.
+
+    J = D_0 * Nx / (|dbc| (Nx-1) Ny Nz) * sum over interior x-faces of g (c[x+1] - c[x]),
+    A lam = dJ/dc, dJ/dg_f = explicit - (lam_u - lam_w)(c_u - c_w) for an interior face,
+    2 lam_u (bc - c_u) for a Dirichlet face (g = hm(k_u, k_u), dg/dk_u = 1), and
+    dg/dk_u = 2 k_w^2 / (k_u + k_w)^2 for g = hm(k_u, k_w). No reference counterpart: the
+    reference solve runs under no_grad (taufactor/taufactor.py:172).
+    """
+    B, X, Y, Z = o.batch_size, o.Nx, o.Ny, o.Nz
+    K = o.D_0 * X / (abs(o.top_bc - o.bot_bc) * (X - 1) * Y * Z)
+    field, _ = solve_fp64(o, rtol=rtol)
+    grads = np.zeros((B, X, Y, Z))
+
+    def dface(a, w):
+        s_ = a + w
+        return np.where(s_ > 0, 2 * w * w / np.where(s_ > 0, s_ * s_, 1.0), 0.0)
+
+    for b in range(B):
+        A, _, keep = assemble(o, b)
+        gx = o.D_x[b, 1:-1].astype(np.float64)  # faces between planes x and x+1
+        dj = np.zeros((X, Y, Z))
+        dj[1:] += gx
+        dj[:-1] -= gx
+        dj *= K
+        lam = np.zeros(X * Y * Z)
+        if len(keep):
+            sol, info = cg(A, dj.ravel()[keep], rtol=rtol, atol=0.0, maxiter=200000,
+                           M=sp.diags(1.0 / A.diagonal()))
+            if info != 0:
+                raise RuntimeError("adjoint CG did not converge")
+            lam[keep] = sol
+        lam = lam.reshape(X, Y, Z)
+        c = field[b]
+        k = o.kappa[b].astype(np.float64)
+        g = np.zeros((X, Y, Z))
+        # x faces: u at x, w at x+1; the explicit term K (c_w - c_u) is the face's flux weight
+        du = c[1:] - c[:-1]
+        djg = K * du - (lam[:-1] - lam[1:]) * (c[:-1] - c[1:])
+        g[:-1] += djg * dface(k[:-1], k[1:])
+        g[1:] += djg * dface(k[1:], k[:-1])
+        g[0] += 2 * lam[0] * (o.top_bc - c[0])
+        g[-1] += 2 * lam[-1] * (o.bot_bc - c[-1])
+        for ax in (1, 2):
+            if o.periodic:
+                cw, lw, kw = np.roll(c, -1, axis=ax), np.roll(lam, -1, axis=ax), np.roll(k, -1, axis=ax)
+                djf = -(lam - lw) * (c - cw)
+                g += djf * dface(k, kw)
+                g += np.roll(djf * dface(kw, k), 1, axis=ax)
+            else:
+                su = tuple(slice(None, -1) if i == ax else slice(None) for i in range(3))
+                sw = tuple(slice(1, None) if i == ax else slice(None) for i in range(3))
+                djf = -(lam[su] - lam[sw]) * (c[su] - c[sw])
+                g[su] += djf * dface(k[su], k[sw])
+                g[sw] += djf * dface(k[sw], k[su])
+        grads[b] = g
+    return grads

@@ -37,7 +37,7 @@ from .percolation import spans_axis0
 
 F32 = np.float32
 
-KINDS = ("binary", "periodic", "anisotropic", "multiphase", "periodic_multiphase")
+KINDS = ("binary", "periodic", "anisotropic", "multiphase", "periodic_multiphase", "kappa", "periodic_kappa")
 
 
 def expand_to_4d(img) -> np.ndarray:
@@ -186,10 +186,19 @@ class OracleSolve:
         if omega is None:
             omega = default_omega(self.Nx)
         self.omega = omega
-        self.periodic = kind in ("periodic", "periodic_multiphase")
-        self.multiphase = kind in ("multiphase", "periodic_multiphase")
+        self.periodic = kind in ("periodic", "periodic_multiphase", "periodic_kappa")
+        self.multiphase = kind in ("multiphase", "periodic_multiphase", "kappa", "periodic_kappa")
         img32 = self.cpu_img.astype(F32)
-        if self.multiphase:
+        if kind in ("kappa", "periodic_kappa"):
+            # per-voxel float32 diffusivity given directly (MultiPhaseSolver's map, :586-588)
+            self.Ds = {}
+            self.conductive_labels = [1]
+            dmap = img32
+            self.kappa = img32
+            mask = (dmap > 0).astype(F32)
+            self.D_x, self.D_y, self.D_z, self.factor = face_conductances(dmap, self.periodic)
+            self.cpu_img = (dmap > 0).astype(np.uint8)
+        elif self.multiphase:
             ds = dict({0: 0, 1: 1} if diffusivities is None else diffusivities)
             for lbl in np.unique(self.cpu_img):
                 if lbl not in ds:
@@ -216,7 +225,10 @@ class OracleSolve:
         self.field = pad_volume(mask * prof[None, :, None, None],
                                 (2 * self.top_bc, 2 * self.bot_bc)).astype(F32)
         self.cb = chequerboard((self.Nx, self.Ny, self.Nz), omega)
-        if self.multiphase:
+        if kind in ("kappa", "periodic_kappa"):
+            self.D_0 = D_0
+            self.D_mean = img32.astype(np.float64).mean(axis=(1, 2, 3))
+        elif self.multiphase:
             vf = {int(p): np.mean(self.cpu_img == p, axis=(1, 2, 3)) for p in np.unique(self.cpu_img)}
             self.D_0 = D_0
             self.D_mean = np.sum([vf[z] * self.Ds.get(z, 0.0) for z in vf], axis=0)

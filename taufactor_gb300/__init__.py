@@ -7,9 +7,10 @@ surface. The sweeps run as hand-written CUDA kernels of ``lib/libtaufactor_gb300
 its C ABI (``include/taufactor_gb300.h``).
 """
 from .batch import BatchSolve
+from .kappa import DeffFunction, KappaSolver, d_eff
 from .solvers import (AnisotropicSolver, MultiPhaseSolver, PeriodicMultiPhaseSolver, PeriodicSolver,
                       SORSolver, Solver, ThroughTransportSolver)
 
 __all__ = ["Solver", "PeriodicSolver", "AnisotropicSolver", "MultiPhaseSolver", "PeriodicMultiPhaseSolver",
-           "SORSolver", "ThroughTransportSolver", "BatchSolve"]
+           "SORSolver", "ThroughTransportSolver", "BatchSolve", "KappaSolver", "DeffFunction", "d_eff"]
 __version__ = "0.1.0"

@@ -22,7 +22,8 @@ EXPORTS = (
     "tf_layer_sums", "tf_unpack", "tf_repack", "tf_check_small_division", "tf_advance_rhs", "tf_widen_f64",
     "tf_narrow_f64", "tf_axpy_f64", "tf_residual_f64", "tf_layer_sums_f64", "tf_batch_desc_bytes", "tf_batch_tile",
     "tf_batch_describe", "tf_batch_advance", "tf_batch_layer_sums", "tf_batch_check", "tf_batch_tick",
-    "tf_batch_converge_static",
+    "tf_batch_converge_static", "tf_kappa_pack", "tf_kappa_advance", "tf_kappa_layer_sums",
+    "tf_kappa_residual_f64", "tf_kappa_adjoint_rhs", "tf_kappa_gradient", "tf_split_to_natural_f64",
 )
 TF_BATCH_ACTIVE, TF_BATCH_CONVERGED, TF_BATCH_NEEDS_HOST = 0, 1, 2
 
@@ -99,6 +100,13 @@ def load():
         "tf_batch_check": (i32, [vp, i32, vp, TfBatchState, C.c_double, i32, i32, vp]),
         "tf_batch_tick": (i32, [vp, i32, vp]),
         "tf_batch_converge_static": (i32, [vp, vp, i32, i32, i64, i64, TfBatchState, C.c_double, i32, i32, vp]),
+        "tf_kappa_pack": (i32, [G, O, vp, vp, vp, vp, vp]),
+        "tf_kappa_advance": (i32, [G, O, vp, vp, vp, i32, i32, vp]),
+        "tf_kappa_layer_sums": (i32, [G, vp, i32, vp, vp, vp, vp]),
+        "tf_kappa_residual_f64": (i32, [G, O, vp, vp, vp, vp, vp, vp, vp]),
+        "tf_kappa_adjoint_rhs": (i32, [G, vp, vp, C.c_double, vp]),
+        "tf_kappa_gradient": (i32, [G, O, vp, vp, vp, vp, C.c_double, C.c_double, C.c_double, vp]),
+        "tf_split_to_natural_f64": (i32, [G, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

@@ -1,0 +1,420 @@
+// Per-voxel conductivity ("kappa field") operator and its adjoint (sm_103a).
+//
+// MultiPhaseSolver (taufactor.py:508-620) assigns each label a diffusivity and couples voxels
+// through harmonic-mean faces 2ab/(a+b) (:577-596), with the x-ghost planes copying the
+// adjacent voxel (:590-592) and the diagonal `factor` summed in a fixed order (:598-603).
+// Here the diffusivity is an arbitrary float32 per voxel, kappa, stored in the field's split
+// layout (ghost cells 0 on closed faces, wrapped copies on periodic ones). With
+// kappa = D[label] every face, factor and update equals MultiPhaseSolver's bit for bit.
+//
+// k_kappa_sweep      one half-sweep in place (float4 groups of one colour), optional RHS
+// k_kappa_residual   float64 r = b - A c with an explicit float64 right-hand side or the
+//                    Dirichlet terms; per-plane sums of r^2 and b^2
+// k_kappa_layer_sums per-plane float64 sums of face_x * (c[x+1] - c[x]) and of c
+// k_kappa_dJdc       adjoint right-hand side dD_eff/dc (float64)
+// k_kappa_grad       dD_eff/dkappa per voxel from c and the adjoint lambda (float64)
+#include "tf_common.cuh"
+#include "tf_internal.h"
+#include "tf_update.cuh"
+
+namespace tf {
+
+// harmonic face in the reference's float32 order: ((2a) b) / (a + b), 0 when a + b == 0
+__device__ __forceinline__ float hface(float a, float b) {
+    const float den = __fadd_rn(a, b);
+    return den > 0.0f ? __fdiv_rn(__fmul_rn(__fmul_rn(2.0f, a), b), den) : 0.0f;
+}
+
+struct KView {
+    Geo g;
+    __device__ __forceinline__ long long off(int x, int y, int z) const {
+        return (long long)x * g.plane_f + (long long)(y + HY) * g.row_f + (z & 1) * g.ZH + HJ + (z >> 1);
+    }
+};
+
+// The six faces of voxel (x,y,z) and their neighbour values, in the reference's roles.
+struct Faces {
+    float xp, xm, yp, ym, zp, zm;   // conductances
+    float div;                      // factor (inf if 0)
+};
+
+// Neighbour (y, z) index with ghost rows/cells: the split layout already holds periodic copies
+// or zeros within one cell of every face, so plain offsets work for y+-1 and z+-1.
+__device__ __forceinline__ Faces kappa_faces(const float* kp, const KView& v, int x, int y, int z, float kc) {
+    Faces f;
+    f.xm = x > 0 ? hface(kc, kp[v.off(x - 1, y, z)]) : hface(kc, kc);
+    f.xp = x + 1 < v.g.NX ? hface(kc, kp[v.off(x + 1, y, z)]) : hface(kc, kc);
+    f.ym = hface(kc, kp[v.off(x, y - 1, z)]);
+    f.yp = hface(kc, kp[v.off(x, y + 1, z)]);
+    f.zm = hface(kc, kp[v.off(x, y, z - 1)]);
+    f.zp = hface(kc, kp[v.off(x, y, z + 1)]);
+    float d = __fadd_rn(f.xm, f.xp);
+    d = __fadd_rn(d, f.ym);
+    d = __fadd_rn(d, f.yp);
+    d = __fadd_rn(d, f.zm);
+    d = __fadd_rn(d, f.zp);
+    if (x == 0) d = __fadd_rn(d, f.xm);
+    if (x == v.g.NX - 1) d = __fadd_rn(d, f.xp);
+    f.div = d == 0.0f ? __int_as_float(0x7f800000) : d;
+    return f;
+}
+
+// One thread per interior voxel of colour `colour`; in place (neighbours have the other colour,
+// and periodic ghosts are refreshed after the launch, as for the plain binary sweep).
+__global__ void __launch_bounds__(256) k_kappa_sweep(float* __restrict__ c, const float* __restrict__ kp,
+                                                     const float* __restrict__ rhs, const SweepArgs a, int colour) {
+    const Geo& g = a.g;
+    const KView v{g};
+    const long long n = (long long)g.NX * g.NY * ((g.NZ + 1) / 2);
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int hz = (g.NZ + 1) / 2;
+    const int x = (int)(i / ((long long)g.NY * hz));
+    const int rem = (int)(i - (long long)x * g.NY * hz);
+    const int y = rem / hz;
+    const int zz = rem - y * hz;
+    const int z = 2 * zz + ((x + y + colour) & 1);  // the colour-`colour` voxel of this pair
+    if (z >= g.NZ) return;
+    const long long b0 = (long long)blockIdx.y * g.vol_f;
+    float* cb = c + b0;
+    const float* kb = kp + b0;
+    const long long o = v.off(x, y, z);
+    const float kc = kb[o];
+    const Faces f = kappa_faces(kb, v, x, y, z, kc);
+    const float cxp = x + 1 < g.NX ? cb[v.off(x + 1, y, z)] : a.ghi;
+    const float cxm = x > 0 ? cb[v.off(x - 1, y, z)] : a.glo;
+    // taufactor.py:607-612: products, then left-to-right sum
+    float s = __fadd_rn(__fmul_rn(cxp, f.xp), __fmul_rn(cxm, f.xm));
+    s = __fadd_rn(s, __fmul_rn(cb[v.off(x, y + 1, z)], f.yp));
+    s = __fadd_rn(s, __fmul_rn(cb[v.off(x, y - 1, z)], f.ym));
+    s = __fadd_rn(s, __fmul_rn(cb[v.off(x, y, z + 1)], f.zp));
+    s = __fadd_rn(s, __fmul_rn(cb[v.off(x, y, z - 1)], f.zm));
+    if (rhs) s = __fadd_rn(s, rhs[b0 + o]);
+    cb[o] = sor_finish(cb[o], quotient(s, f.div), a.omega);
+}
+
+// float64 residual; bsrc (float64, split layout) replaces the Dirichlet terms when non-null.
+__global__ void __launch_bounds__(256) k_kappa_residual(const double* __restrict__ c64, const float* __restrict__ kp,
+                                                        const double* __restrict__ bsrc, float* __restrict__ r32,
+                                                        double* __restrict__ r2, double* __restrict__ b2, const Geo g,
+                                                        float glo, float ghi) {
+    __shared__ double red[2][32];
+    const KView v{g};
+    const int x = blockIdx.x, b = blockIdx.y;
+    const long long b0 = (long long)b * g.vol_f;
+    const double* cb = c64 + b0;
+    const float* kb = kp + b0;
+    double rs = 0.0, bs = 0.0;
+    for (long long it = threadIdx.x; it < (long long)g.NY * g.NZ; it += blockDim.x) {
+        const int y = (int)(it / g.NZ), z = (int)(it - (long long)y * g.NZ);
+        const long long o = v.off(x, y, z);
+        const Faces f = kappa_faces(kb, v, x, y, z, kb[o]);
+        double res = 0.0, rhs = 0.0;
+        if (f.div < __int_as_float(0x7f800000)) {
+            double s = (double)f.yp * cb[v.off(x, y + 1, z)] + (double)f.ym * cb[v.off(x, y - 1, z)] +
+                       (double)f.zp * cb[v.off(x, y, z + 1)] + (double)f.zm * cb[v.off(x, y, z - 1)];
+            if (x > 0) s += (double)f.xm * cb[v.off(x - 1, y, z)];
+            else if (!bsrc) rhs += (double)f.xm * glo;
+            if (x + 1 < g.NX) s += (double)f.xp * cb[v.off(x + 1, y, z)];
+            else if (!bsrc) rhs += (double)f.xp * ghi;
+            if (bsrc) rhs = bsrc[b0 + o];
+            res = rhs - ((double)f.div * cb[o] - s);
+        }
+        r32[b0 + o] = (float)res;
+        rs += res * res;
+        bs += rhs * rhs;
+    }
+    for (int s = 16; s > 0; s >>= 1) {
+        rs += __shfl_xor_sync(0xffffffffu, rs, s);
+        bs += __shfl_xor_sync(0xffffffffu, bs, s);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        red[0][threadIdx.x >> 5] = rs;
+        red[1][threadIdx.x >> 5] = bs;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double p = 0.0, q = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            p += red[0][w];
+            q += red[1][w];
+        }
+        r2[(long long)b * g.NX + x] = p;
+        b2[(long long)b * g.NX + x] = q;
+    }
+}
+
+// T = float or double field
+template <typename T>
+__global__ void __launch_bounds__(256) k_kappa_layer_sums(const T* __restrict__ c, const float* __restrict__ kp,
+                                                          double* __restrict__ flux, double* __restrict__ csum,
+                                                          const Geo g) {
+    __shared__ double red[2][32];
+    const KView v{g};
+    const int x = blockIdx.x, b = blockIdx.y;
+    const long long b0 = (long long)b * g.vol_f;
+    const bool has_flux = x + 1 < g.NX;
+    double fs = 0.0, cs = 0.0;
+    for (long long it = threadIdx.x; it < (long long)g.NY * g.NZ; it += blockDim.x) {
+        const int y = (int)(it / g.NZ), z = (int)(it - (long long)y * g.NZ);
+        const long long o = v.off(x, y, z);
+        const T a = c[b0 + o];
+        cs += (double)a;
+        if (has_flux) {
+            const long long o1 = v.off(x + 1, y, z);
+            const float face = hface(kp[b0 + o], kp[b0 + o1]);
+            if (sizeof(T) == 4)
+                fs += (double)__fmul_rn(face, __fsub_rn((float)c[b0 + o1], (float)a));  // :617-619 in float32
+            else
+                fs += (double)face * ((double)c[b0 + o1] - (double)a);
+        }
+    }
+    for (int s = 16; s > 0; s >>= 1) {
+        fs += __shfl_xor_sync(0xffffffffu, fs, s);
+        cs += __shfl_xor_sync(0xffffffffu, cs, s);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        red[0][threadIdx.x >> 5] = fs;
+        red[1][threadIdx.x >> 5] = cs;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double p = 0.0, q = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            p += red[0][w];
+            q += red[1][w];
+        }
+        if (has_flux) flux[(long long)b * (g.NX - 1) + x] = p;
+        csum[(long long)b * g.NX + x] = q;
+    }
+}
+
+// dJ/dc for J = D_0 * mean_x(layer flux) * Nx / |bc_hi - bc_lo| with layer flux
+// (1/(Ny Nz)) sum face_x (c[x+1] - c[x]): dJ/dc[x] = K (face_{x-1|x} - face_{x|x+1}),
+// K = D_0 Nx / (|dbc| (Nx-1) Ny Nz). Written for interior voxels (0 elsewhere).
+__global__ void k_kappa_dJdc(const float* __restrict__ kp, double* __restrict__ g_out, const Geo g, double K) {
+    const KView v{g};
+    const long long n = (long long)g.NX * g.NY * g.NZ;
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int x = (int)(i / ((long long)g.NY * g.NZ));
+    const int rem = (int)(i - (long long)x * g.NY * g.NZ);
+    const int y = rem / g.NZ, z = rem - (rem / g.NZ) * g.NZ;
+    const long long b0 = (long long)blockIdx.y * g.vol_f;
+    const long long o = v.off(x, y, z);
+    const float kc = kp[b0 + o];
+    double d = 0.0;
+    if (x > 0) d += (double)hface(kp[b0 + v.off(x - 1, y, z)], kc);
+    if (x + 1 < g.NX) d -= (double)hface(kc, kp[b0 + v.off(x + 1, y, z)]);
+    g_out[b0 + o] = K * d;
+}
+
+// d hface(a, b) / d a = 2 b^2 / (a + b)^2 (0 if a + b == 0), in float64
+__device__ __forceinline__ double dface_da(double a, double b) {
+    const double s = a + b;
+    return s > 0.0 ? 2.0 * b * b / (s * s) : 0.0;
+}
+
+// dJ/dkappa[u] = sum over u's faces f of dJ/dg_f * dg_f/dkappa_u, with
+//   interior face (u,w): dJ/dg = explicit - (lam_u - lam_w)(c_u - c_w),
+//                        explicit = K (c[x+1] - c[x]) for x-faces between two interior planes;
+//   Dirichlet face of u (x = 0 or Nx-1, conductance hface(k_u, k_u), counted twice in A and b):
+//                        dJ/dg = 2 lam_u (bc - c_u), dg/dk_u = d/dk hface(k, k) = 1.
+// Out: natural layout [b][x][y][z] float64.
+__global__ void k_kappa_grad(const double* __restrict__ c64, const double* __restrict__ lam,
+                             const float* __restrict__ kp, double* __restrict__ grad, const Geo g, int periodic,
+                             double K, double bc_lo, double bc_hi) {
+    const KView v{g};
+    const long long n = (long long)g.NX * g.NY * g.NZ;
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int x = (int)(i / ((long long)g.NY * g.NZ));
+    const int rem = (int)(i - (long long)x * g.NY * g.NZ);
+    const int y = rem / g.NZ, z = rem - y * g.NZ;
+    const long long b0 = (long long)blockIdx.y * g.vol_f;
+    const long long o = v.off(x, y, z);
+    const double ku = kp[b0 + o], cu = c64[b0 + o], lu = lam[b0 + o];
+    double gr = 0.0;
+    // x faces
+    if (x > 0) {
+        const long long w = v.off(x - 1, y, z);
+        const double kw = kp[b0 + w], cw = c64[b0 + w], lw = lam[b0 + w];
+        const double dj = K * (cu - cw) - (lu - lw) * (cu - cw);
+        gr += dj * dface_da(ku, kw);
+    } else {
+        gr += 2.0 * lu * (bc_lo - cu);
+    }
+    if (x + 1 < g.NX) {
+        const long long w = v.off(x + 1, y, z);
+        const double kw = kp[b0 + w], cw = c64[b0 + w], lw = lam[b0 + w];
+        const double dj = K * (cw - cu) - (lu - lw) * (cu - cw);
+        gr += dj * dface_da(ku, kw);
+    } else {
+        gr += 2.0 * lu * (bc_hi - cu);
+    }
+    // y and z faces (neighbours outside closed faces have kappa 0 -> face 0, derivative 0)
+    const int dy[4] = {1, -1, 0, 0}, dz[4] = {0, 0, 1, -1};
+    for (int k = 0; k < 4; ++k) {
+        int yy = y + dy[k], zq = z + dz[k];
+        if (yy < 0 || yy >= g.NY) {
+            if (!(periodic & TF_PERIODIC_Y)) continue;
+            yy = wrap(yy, g.NY);
+        }
+        if (zq < 0 || zq >= g.NZ) {
+            if (!(periodic & TF_PERIODIC_Z)) continue;
+            zq = wrap(zq, g.NZ);
+        }
+        const long long w = v.off(x, yy, zq);
+        const double kw = kp[b0 + w], cw = c64[b0 + w], lw = lam[b0 + w];
+        gr += -(lu - lw) * (cu - cw) * dface_da(ku, kw);
+    }
+    grad[(long long)blockIdx.y * n + i] = gr;
+}
+
+}  // namespace tf
+
+// ------------------------------------------------------------------------------ host side
+namespace tf {
+
+// kappa natural [b][x][y][z] -> split layout with ghost cells (0 on closed faces, wrapped
+// copies on periodic ones); initial field = profile[x] where kappa > 0 (taufactor.py:282-291
+// with MultiPhaseSolver's conductive mask, :571-575).
+__global__ void k_kappa_pack(const float* __restrict__ kin, const float* __restrict__ profile,
+                             float* __restrict__ kout, float* __restrict__ field, const Geo g, int periodic) {
+    const int pos = blockIdx.x * blockDim.x + threadIdx.x;  // q*ZH + jp
+    if (pos >= 2 * g.ZH) return;
+    const int Y = blockIdx.y, bx = blockIdx.z;
+    const int x = bx % g.NX, b = bx / g.NX;
+    const int q = pos >= g.ZH ? 1 : 0;
+    const int jp = pos - q * g.ZH;
+    int y = Y - HY, z = 2 * (jp - HJ) + q;
+    float kv = 0.0f, fv = 0.0f;
+    bool ok = true;
+    if (y < 0 || y >= g.NY) {
+        ok = ok && (periodic & TF_PERIODIC_Y);
+        y = wrap(y, g.NY);
+    }
+    if (z < 0 || z >= g.NZ) {
+        ok = ok && (periodic & TF_PERIODIC_Z);
+        z = wrap(z, g.NZ);
+    }
+    if (ok) {
+        kv = kin[(((long long)b * g.NX + x) * g.NY + y) * g.NZ + z];
+        fv = kv > 0.0f ? profile[x] : 0.0f;
+    }
+    const long long o = ((long long)bx * g.YP + Y) * 2 * g.ZH + pos;
+    kout[o] = kv;
+    field[o] = fv;
+}
+
+// split layout (float64) -> natural [b][x][y][z] (float64)
+__global__ void k_split_to_natural(const double* __restrict__ in, double* __restrict__ out, const Geo g) {
+    const long long n = (long long)g.NX * g.NY * g.NZ;
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int x = (int)(i / ((long long)g.NY * g.NZ));
+    const int rem = (int)(i - (long long)x * g.NY * g.NZ);
+    const int y = rem / g.NZ, z = rem - y * g.NZ;
+    const KView v{g};
+    out[(long long)blockIdx.y * n + i] = in[(long long)blockIdx.y * g.vol_f + v.off(x, y, z)];
+}
+
+}  // namespace tf
+
+using namespace tf;
+
+extern "C" {
+
+int tf_kappa_pack(const tf_geom* g, const tf_operator* op, const float* kappa_dev, const float* profile_dev,
+                  float* kappa_split_dev, float* field_dev, void* stream) {
+    if (!g || !op || !kappa_dev || !profile_dev || !kappa_split_dev || !field_dev) return TF_ERR_ARG;
+    const Geo geo = make_geo(*g);
+    dim3 grid((2 * g->zh + 127) / 128, g->yp, g->batch * g->nx);
+    k_kappa_pack<<<grid, 128, 0, (cudaStream_t)stream>>>(kappa_dev, profile_dev, kappa_split_dev, field_dev, geo,
+                                                         op->periodic);
+    note_launch();
+    return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
+}
+
+int tf_kappa_advance(const tf_geom* g, const tf_operator* op, float* field_dev, const float* kappa_split_dev,
+                     const float* rhs_dev, int first_colour, int n_half, void* stream) {
+    if (!g || !op || !field_dev || !kappa_split_dev || n_half < 0) return TF_ERR_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    const Geo geo = make_geo(*g);
+    const long long n = (long long)g->nx * g->ny * ((g->nz + 1) / 2);
+    dim3 grid((unsigned)((n + 255) / 256), g->batch);
+    int colour = first_colour & 1;
+    for (int i = 0; i < n_half; ++i, colour ^= 1) {
+        SweepArgs a = make_args(geo, *op, field_dev, colour, 1, nullptr);
+        k_kappa_sweep<<<grid, 256, 0, st>>>(field_dev, kappa_split_dev, rhs_dev, a, colour);
+        note_launch();
+        if (cudaGetLastError() != cudaSuccess) return TF_ERR_CUDA;
+        if (op->periodic) {
+            const int rc = refresh_ghosts(*g, op->periodic, field_dev, st);
+            if (rc) return rc;
+        }
+    }
+    return TF_OK;
+}
+
+int tf_kappa_layer_sums(const tf_geom* g, const void* field_dev, int field_is_f64, const float* kappa_split_dev,
+                        double* flux_sum_dev, double* c_sum_dev, void* stream) {
+    if (!g || !field_dev || !kappa_split_dev || !c_sum_dev || (g->nx > 1 && !flux_sum_dev)) return TF_ERR_ARG;
+    const Geo geo = make_geo(*g);
+    dim3 grid(g->nx, g->batch);
+    if (field_is_f64)
+        k_kappa_layer_sums<double><<<grid, 256, 0, (cudaStream_t)stream>>>(
+            static_cast<const double*>(field_dev), kappa_split_dev, flux_sum_dev, c_sum_dev, geo);
+    else
+        k_kappa_layer_sums<float><<<grid, 256, 0, (cudaStream_t)stream>>>(
+            static_cast<const float*>(field_dev), kappa_split_dev, flux_sum_dev, c_sum_dev, geo);
+    note_launch();
+    return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
+}
+
+int tf_kappa_residual_f64(const tf_geom* g, const tf_operator* op, const double* field64_dev,
+                          const float* kappa_split_dev, const double* b64_dev, float* rhs_dev, double* r2_sum_dev,
+                          double* b2_sum_dev, void* stream) {
+    if (!g || !op || !field64_dev || !kappa_split_dev || !rhs_dev || !r2_sum_dev || !b2_sum_dev) return TF_ERR_ARG;
+    const Geo geo = make_geo(*g);
+    k_kappa_residual<<<dim3(g->nx, g->batch), 256, 0, (cudaStream_t)stream>>>(
+        field64_dev, kappa_split_dev, b64_dev, rhs_dev, r2_sum_dev, b2_sum_dev, geo, op->ghost_lo, op->ghost_hi);
+    note_launch();
+    if (cudaGetLastError() != cudaSuccess) return TF_ERR_CUDA;
+    return op->periodic ? refresh_ghosts(*g, op->periodic, rhs_dev, (cudaStream_t)stream) : TF_OK;
+}
+
+int tf_kappa_adjoint_rhs(const tf_geom* g, const float* kappa_split_dev, double* out64_dev, double scale,
+                         void* stream) {
+    if (!g || !kappa_split_dev || !out64_dev) return TF_ERR_ARG;
+    const Geo geo = make_geo(*g);
+    const long long n = (long long)g->nx * g->ny * g->nz;
+    k_kappa_dJdc<<<dim3((unsigned)((n + 255) / 256), g->batch), 256, 0, (cudaStream_t)stream>>>(kappa_split_dev,
+                                                                                                out64_dev, geo, scale);
+    note_launch();
+    return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
+}
+
+int tf_kappa_gradient(const tf_geom* g, const tf_operator* op, const double* field64_dev, const double* lambda64_dev,
+                      const float* kappa_split_dev, double* grad_dev, double scale, double bc_lo, double bc_hi,
+                      void* stream) {
+    if (!g || !op || !field64_dev || !lambda64_dev || !kappa_split_dev || !grad_dev) return TF_ERR_ARG;
+    const Geo geo = make_geo(*g);
+    const long long n = (long long)g->nx * g->ny * g->nz;
+    k_kappa_grad<<<dim3((unsigned)((n + 255) / 256), g->batch), 256, 0, (cudaStream_t)stream>>>(
+        field64_dev, lambda64_dev, kappa_split_dev, grad_dev, geo, op->periodic, scale, bc_lo, bc_hi);
+    note_launch();
+    return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
+}
+
+int tf_split_to_natural_f64(const tf_geom* g, const double* split_dev, double* natural_dev, void* stream) {
+    if (!g || !split_dev || !natural_dev) return TF_ERR_ARG;
+    const Geo geo = make_geo(*g);
+    const long long n = (long long)g->nx * g->ny * g->nz;
+    k_split_to_natural<<<dim3((unsigned)((n + 255) / 256), g->batch), 256, 0, (cudaStream_t)stream>>>(
+        split_dev, natural_dev, geo);
+    note_launch();
+    return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
+}
+
+}  // extern "C"

@@ -1,0 +1,246 @@
+"""Per-voxel conductivity solve with adjoint gradients (no reference counterpart as an API).
+
+``MultiPhaseSolver`` (taufactor/taufactor.py:508-620) gives every label a diffusivity and couples
+voxels by harmonic-mean faces. ``KappaSolver`` takes the diffusivity per voxel directly, a
+float32 field kappa >= 0; with kappa = D[label] its faces, factor and half-sweeps equal
+``MultiPhaseSolver``'s bit for bit (tests/test_adjoint_gpu.py checks this).
+
+On top of the forward solve (the reference's iteration and convergence rule, plus FP64 defect
+correction) it computes dD_eff/dkappa by the adjoint method: the operator is symmetric, so the
+adjoint A lam = dD_eff/dc is solved by the same sweeps with a right-hand side, again with FP64
+defect correction, and the gradient is assembled per voxel from c and lam on the device. Only
+the converged c is kept for the backward pass (``DeffFunction``, a torch.autograd.Function).
+
+The reference runs its solve under ``torch.no_grad()`` (taufactor.py:172); gradients are pinned
+by central finite differences and by an FP64 adjoint on the CPU (``oracle/fp64.py``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+from timeit import default_timer as timer
+
+import numpy as np
+import torch
+
+from . import _capi
+from ._capi import TF_KIND_MULTIPHASE, TF_PERIODIC_Y, TF_PERIODIC_Z, TfGeom, TfOperator, check
+from .solvers import layer_metrics
+
+
+def _ptr(t: torch.Tensor) -> int:
+    return t.data_ptr()
+
+
+class KappaSolver:
+    """Through-transport solve on a per-voxel conductivity field.
+
+    kappa     float array [X,Y,Z] or [B,X,Y,Z] (numpy or torch), values >= 0
+    periodic  periodic in y and z (as PeriodicMultiPhaseSolver)
+    omega     over-relaxation factor (default: the reference's 2 - pi/(1.5 Nx))
+    D_0       scaling of D_eff (MultiPhaseSolver's D_scaling)
+    """
+
+    top_bc, bot_bc = -0.5, 0.5
+
+    def __init__(self, kappa, periodic: bool = False, omega=None, D_0=1.0, device="cuda"):
+        self.device = torch.device(device)
+        if self.device.type != "cuda" or not torch.cuda.is_available():
+            raise RuntimeError("KappaSolver runs on CUDA devices only")
+        if self.device.index is None:
+            self.device = torch.device("cuda", torch.cuda.current_device())
+        k = torch.as_tensor(kappa, dtype=torch.float32)
+        if k.dim() == 3:
+            k = k[None]
+        if k.dim() != 4:
+            raise ValueError("kappa must be [X,Y,Z] or [B,X,Y,Z]")
+        if not torch.isfinite(k).all() or (k < 0).any():
+            raise ValueError("kappa must be finite and >= 0")
+        self.batch_size, self.Nx, self.Ny, self.Nz = k.shape
+        if self.Nx < 2:
+            raise ValueError("need at least two planes along x")
+        self.kappa = k.to(self.device).contiguous()
+        self.periodic = bool(periodic)
+        self.omega = 2 - math.pi / (1.5 * self.Nx) if omega is None else omega
+        self.D_0 = D_0
+        kc = self.kappa.double()
+        mask = kc > 0
+        self.vol_x = mask.double().mean(dim=(2, 3)).cpu().numpy()
+        self.D_mean = kc.mean(dim=(1, 2, 3)).cpu().numpy()
+        self.cpu_img = None  # built lazily for the percolation fallback
+        self.conductive_labels = [1]
+        self._lib = lib = _capi.load()
+        g = self._geom = TfGeom()
+        pflag = (TF_PERIODIC_Y | TF_PERIODIC_Z) if self.periodic else 0
+        check(lib.tf_geometry(self.batch_size, self.Nx, self.Ny, self.Nz, pflag, C.byref(g)), "tf_geometry")
+        op = self._op = TfOperator()
+        op.kind = TF_KIND_MULTIPHASE
+        op.periodic = pflag
+        op.omega = float(np.float32(self.omega))
+        op.ghost_lo, op.ghost_hi = 2 * self.top_bc, 2 * self.bot_bc
+        op.ky = op.kz = 1.0
+        op.n_phases = 1
+        with torch.cuda.device(self.device):
+            st = self._stream()
+            self._ks = torch.empty(g.field_elems, dtype=torch.float32, device=self.device)
+            self._c = torch.empty(g.field_elems, dtype=torch.float32, device=self.device)
+            sh = 1 / (2 * self.Nx)
+            prof = torch.linspace(self.top_bc + sh, self.bot_bc - sh, self.Nx, dtype=torch.float32).to(self.device)
+            check(lib.tf_kappa_pack(C.byref(g), C.byref(op), _ptr(self.kappa), _ptr(prof), _ptr(self._ks),
+                                    _ptr(self._c), st), "tf_kappa_pack")
+            self._flux = torch.empty((self.batch_size, self.Nx - 1), dtype=torch.float64, device=self.device)
+            self._csum = torch.empty((self.batch_size, self.Nx), dtype=torch.float64, device=self.device)
+        self._c64 = None
+        self.iter = 0
+        self.converged = False
+        self.old_tau = 0
+        self.tau = self.D_eff = self.tau_x = None
+        self.walltime = 0.0
+        self.timings = {}
+
+    def _stream(self):
+        return torch.cuda.current_stream(self.device).cuda_stream
+
+    # ---------------------------------------------------------------- forward
+    def _advance(self, n: int, field: torch.Tensor, rhs=None, op=None, first_colour=None):
+        check(self._lib.tf_kappa_advance(C.byref(self._geom), C.byref(op or self._op), _ptr(field), _ptr(self._ks),
+                                         _ptr(rhs) if rhs is not None else None,
+                                         self.iter % 2 if first_colour is None else first_colour, n,
+                                         self._stream()), "tf_kappa_advance")
+
+    def _layer_means(self):
+        f, is64 = (self._c64, 1) if self._c64 is not None else (self._c, 0)
+        check(self._lib.tf_kappa_layer_sums(C.byref(self._geom), _ptr(f), is64, _ptr(self._ks), _ptr(self._flux),
+                                            _ptr(self._csum), self._stream()), "tf_kappa_layer_sums")
+        area = float(self.Ny * self.Nz)
+        return self._flux.cpu().numpy() / area, self._csum.cpu().numpy() / area
+
+    def compute_metrics(self):
+        if self.cpu_img is None:
+            self.cpu_img = (self.kappa > 0).to(torch.uint8).cpu().numpy()
+        self.flux_1d, c_x = self._layer_means()
+        return layer_metrics(self, self.flux_1d, c_x)
+
+    def solve(self, iter_limit=10000, conv_crit=1e-2, verbose=False, refine=False):
+        """The reference's loop and convergence rule (taufactor.py:156-191) on this operator."""
+        start = timer()
+        with torch.cuda.device(self.device):
+            while not self.converged and self.iter < iter_limit:
+                n = min(100 - self.iter % 100, iter_limit - self.iter)
+                self._c64 = None
+                self._advance(n, self._c)
+                self.iter += n
+                if self.iter % 100 == 0:
+                    self.tau, rel = self.compute_metrics()
+                    if verbose:
+                        print(f"Iter: {self.iter}, conv error: {np.max(np.abs(rel)):.3E}")
+                    if np.all(rel < conv_crit) and np.max(np.abs(self.tau - self.old_tau)) < 2e-3:
+                        self.converged = True
+                    else:
+                        self.old_tau = self.tau
+            if refine:
+                self.refine(**(refine if isinstance(refine, dict) else {}))
+            torch.cuda.synchronize(self.device)
+        self.walltime = timer() - start
+        self.tau = np.where(self.tau == 0, np.inf, self.tau)
+        return self.tau_x
+
+    def _fp64_solve(self, x64, b64, tol, max_outer, n_inner):
+        """FP64 defect correction for A x = b (b64 None: the Dirichlet terms); returns history."""
+        g, lib, st = self._geom, self._lib, self._stream()
+        op0 = TfOperator.from_buffer_copy(self._op)
+        op0.ghost_lo = op0.ghost_hi = 0.0
+        rhs = torch.zeros(g.field_elems, dtype=torch.float32, device=self.device)
+        e = torch.zeros_like(rhs)
+        r2 = torch.empty((self.batch_size, self.Nx), dtype=torch.float64, device=self.device)
+        b2 = torch.empty_like(r2)
+        hist = []
+        for outer in range(max_outer + 1):
+            check(lib.tf_kappa_residual_f64(C.byref(g), C.byref(self._op), _ptr(x64), _ptr(self._ks),
+                                            _ptr(b64) if b64 is not None else None, _ptr(rhs), _ptr(r2), _ptr(b2),
+                                            st), "tf_kappa_residual_f64")
+            rel = float((torch.sqrt(r2.sum(dim=1)) / torch.sqrt(b2.sum(dim=1)).clamp_min(1e-300)).max().item())
+            hist.append(rel)
+            if rel < tol or outer == max_outer:
+                break
+            e.zero_()
+            self._advance(n_inner, e, rhs=rhs, op=op0, first_colour=0)
+            check(lib.tf_axpy_f64(C.byref(g), _ptr(x64), _ptr(e), st), "tf_axpy_f64")
+        return hist
+
+    def refine(self, tol: float = 1e-11, max_outer: int = 12, inner_half_sweeps=None):
+        """FP64 defect correction of the converged field; metrics from the float64 field."""
+        t0 = timer()
+        n_inner = inner_half_sweeps or max(400, 2 * (self.iter or 200))
+        with torch.cuda.device(self.device):
+            g, lib, st = self._geom, self._lib, self._stream()
+            c64 = torch.empty(g.field_elems, dtype=torch.float64, device=self.device)
+            check(lib.tf_widen_f64(C.byref(g), _ptr(self._c), _ptr(c64), st), "tf_widen_f64")
+            self.residual_history = self._fp64_solve(c64, None, tol, max_outer, n_inner)
+            check(lib.tf_narrow_f64(C.byref(g), C.byref(self._op), _ptr(c64), _ptr(self._c), st), "tf_narrow_f64")
+            self._c64 = c64
+            self.tau, _ = self.compute_metrics()
+            torch.cuda.synchronize(self.device)
+        self.tau = np.where(self.tau == 0, np.inf, self.tau)
+        self.timings["refine_s"] = timer() - t0
+        return self.residual_history
+
+    # ---------------------------------------------------------------- adjoint
+    def gradient(self, tol: float = 1e-11, max_outer: int = 12, inner_half_sweeps=None) -> torch.Tensor:
+        """dD_eff/dkappa [B,X,Y,Z] (float64, on the device) at the current (refined) solution."""
+        if self._c64 is None:
+            self.refine(tol=tol)
+        t0 = timer()
+        n_inner = inner_half_sweeps or max(400, 2 * (self.iter or 200))
+        scale = self.D_0 * self.Nx / (abs(self.bot_bc - self.top_bc) * (self.Nx - 1) * self.Ny * self.Nz)
+        with torch.cuda.device(self.device):
+            g, lib, st = self._geom, self._lib, self._stream()
+            dj = torch.zeros(g.field_elems, dtype=torch.float64, device=self.device)
+            check(lib.tf_kappa_adjoint_rhs(C.byref(g), _ptr(self._ks), _ptr(dj), float(scale), st),
+                  "tf_kappa_adjoint_rhs")
+            lam = torch.zeros(g.field_elems, dtype=torch.float64, device=self.device)
+            self.adjoint_history = self._fp64_solve(lam, dj, tol, max_outer, n_inner)
+            grad = torch.empty((self.batch_size, self.Nx, self.Ny, self.Nz), dtype=torch.float64, device=self.device)
+            check(lib.tf_kappa_gradient(C.byref(g), C.byref(self._op), _ptr(self._c64), _ptr(lam), _ptr(self._ks),
+                                        _ptr(grad), float(scale), float(self.top_bc), float(self.bot_bc), st),
+                  "tf_kappa_gradient")
+            torch.cuda.synchronize(self.device)
+        self.timings["adjoint_s"] = timer() - t0
+        return grad
+
+    def field(self) -> torch.Tensor:
+        """The float32 field in the reference's padded layout [B,Nx+2,Ny+2,Nz+2]."""
+        out = torch.empty((self.batch_size, self.Nx + 2, self.Ny + 2, self.Nz + 2), dtype=torch.float32,
+                          device=self.device)
+        with torch.cuda.device(self.device):
+            check(self._lib.tf_unpack(C.byref(self._geom), C.byref(self._op), _ptr(self._c), _ptr(out),
+                                      self._stream()), "tf_unpack")
+        return out
+
+
+class DeffFunction(torch.autograd.Function):
+    """D_eff(kappa) as a differentiable torch op: forward = converged, FP64-refined solve;
+    backward = adjoint solve. Saves only the solver with its converged field."""
+
+    @staticmethod
+    def forward(ctx, kappa: torch.Tensor, periodic: bool = False, conv_crit: float = 1e-3, tol: float = 1e-11):
+        s = KappaSolver(kappa.detach(), periodic=periodic, device=kappa.device)
+        s.solve(conv_crit=conv_crit, refine={"tol": tol})
+        ctx.solver = s
+        ctx.tol = tol
+        ctx.squeeze = kappa.dim() == 3
+        d = torch.as_tensor(np.asarray(s.D_eff, dtype=np.float64), device=kappa.device)
+        return d[0] if ctx.squeeze else d
+
+    @staticmethod
+    def backward(ctx, grad_out):
+        s = ctx.solver
+        g = s.gradient(tol=ctx.tol)
+        go = grad_out.reshape(-1, 1, 1, 1).to(g.dtype)
+        grad = (g * go).to(torch.float32)
+        return (grad[0] if ctx.squeeze else grad), None, None, None
+
+
+def d_eff(kappa: torch.Tensor, periodic: bool = False, conv_crit: float = 1e-3, tol: float = 1e-11) -> torch.Tensor:
+    """Differentiable D_eff of a per-voxel conductivity field (float64 result)."""
+    return DeffFunction.apply(kappa, periodic, conv_crit, tol)

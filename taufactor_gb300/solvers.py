@@ -582,6 +582,30 @@ class MultiPhaseSolver(ThroughTransportSolver):
         return op
 
 
+    def phase_gradients(self, conv_crit: float = 1e-3, tol: float = 1e-11) -> dict:
+        """dD_eff/dD_p for every label p (numpy [B] per label), by the adjoint method.
+
+        Builds the per-voxel field kappa = D[label] (float32, the same faces as this solver,
+        bit for bit), solves it to the reference's rule plus FP64 defect correction, solves the
+        adjoint and sums dD_eff/dkappa over the voxels of each label. No reference counterpart
+        (the reference solve runs under no_grad, taufactor.py:172).
+        """
+        from .kappa import KappaSolver
+
+        lab = torch.from_numpy(np.ascontiguousarray(self.cpu_img)).to(self.device)
+        kap = torch.zeros(lab.shape, dtype=torch.float32, device=self.device)
+        for p in unique_labels(self.cpu_img):
+            kap[lab == p] = float(F32(self.Ds.get(int(p), 0.0)))
+        ks = KappaSolver(kap, periodic=bool(self._periodic), omega=self.omega, D_0=self.D_0, device=self.device)
+        ks.solve(conv_crit=conv_crit, refine={"tol": tol})
+        g = ks.gradient(tol=tol)
+        self.kappa_solver = ks
+        out = {}
+        for p in unique_labels(self.cpu_img):
+            out[int(p)] = (g * (lab == p)).sum(dim=(1, 2, 3)).cpu().numpy()
+        return out
+
+
 class PeriodicMultiPhaseSolver(MultiPhaseSolver):
     """Multiphase, periodic in y and z (taufactor.py:623-656)."""
 
