@@ -296,6 +296,111 @@ def run_ours(args):
         torch.distributed.destroy_process_group()
 
 
+def uneven_batch(dev, conv_crit=CONV_CRIT, repeat=2):
+    """64 volumes with sides from {64..256} (half PeriodicSolver): batched solve (one graph per
+    200 half-sweeps, device-side convergence) vs the plain per-volume loop of drop-in solvers.
+    Both reach the same per-volume results; reported as converged solves/s."""
+    import torch
+
+    import taufactor_gb300 as tg
+    from taufactor_gb300.synthetic import uneven_volumes
+
+    vols = uneven_volumes(64)
+    periodic = [i % 2 == 1 for i in range(len(vols))]
+    voxels = sum(v.size for v in vols)
+    b = tg.BatchSolve(vols, periodic=periodic, device=dev)
+    b.solve(conv_crit=conv_crit)  # warm-up (graph capture)
+    t_batch = []
+    for _ in range(repeat):
+        b = tg.BatchSolve(vols, periodic=periodic, device=dev)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = b.solve(conv_crit=conv_crit)
+        torch.cuda.synchronize()
+        t_batch.append(time.perf_counter() - t0)
+    iters = [r.iter for r in res]
+    d_batch = np.array([r.D_eff[0] for r in res])
+    solvers = [(tg.PeriodicSolver if p else tg.Solver)(v, device=dev) for v, p in zip(vols, periodic)]
+    for s in solvers[:4]:
+        s.solve(verbose=False, conv_crit=conv_crit)  # warm-up
+    solvers = [(tg.PeriodicSolver if p else tg.Solver)(v, device=dev) for v, p in zip(vols, periodic)]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    d_loop = []
+    for s in solvers:
+        s.solve(verbose=False, conv_crit=conv_crit)
+        d_loop.append(s.D_eff[0])
+    torch.cuda.synchronize()
+    t_loop = time.perf_counter() - t0
+    tb = min(t_batch)
+    vu = sum(it * v.size / 2 for it, v in zip(iters, vols))
+    return {"workload": "64 volumes, sides from {64,96,128,192,256}, blurred noise sigma=2, porosity U[0.35,0.70], "
+                        "half PeriodicSolver", "voxels": int(voxels), "conv_crit": conv_crit,
+            "batched_solves_per_s": 64 / tb, "per_volume_loop_solves_per_s": 64 / t_loop,
+            "speedup": t_loop / tb, "batched_voxel_updates_per_s": vu / tb,
+            "max_rel_D_eff_batched_vs_loop": float(np.max(np.abs(d_batch - np.array(d_loop)) /
+                                                          np.abs(np.array(d_loop)))),
+            "timing": "wall clock incl. set-up of the solver objects' loop, excl. input generation"}
+
+
+def adjoint_cost(dev, side=320, fd_voxels=0, tol=1e-12, fd_tol=1e-14):
+    """Per-voxel conductivity kappa = sigmoid(blur_2(2 N(0,1))) on side^3 (default_rng(3003)):
+    forward solve + FP64 refinement, then the adjoint gradient; times and, with fd_voxels > 0,
+    central finite differences (h = 1e-3) on random voxels (default_rng(3004))."""
+    import torch
+    from scipy.ndimage import gaussian_filter
+
+    import taufactor_gb300 as tg
+
+    logits = gaussian_filter(2.0 * np.random.default_rng(3003).standard_normal((side,) * 3, dtype=np.float32), 2.0)
+    kap = (1.0 / (1.0 + np.exp(-logits))).astype(np.float32)
+    s = tg.KappaSolver(kap, device=dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s.solve(conv_crit=1e-3, refine={"tol": tol})
+    torch.cuda.synchronize()
+    t_fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    g = s.gradient(tol=tol)
+    torch.cuda.synchronize()
+    t_adj = time.perf_counter() - t0
+    out = {"workload": f"kappa field {side}^3 = sigmoid(blur_sigma2(2 N(0,1)))", "forward_s": t_fwd,
+           "adjoint_s": t_adj, "adjoint_over_forward": t_adj / t_fwd, "half_sweeps_forward": s.iter,
+           "fp64_residual": s.residual_history[-1], "adjoint_residual": s.adjoint_history[-1],
+           "D_eff": float(s.D_eff[0]),
+           # D_eff is homogeneous of degree 1 in kappa, so sum(kappa * dD_eff/dkappa) = D_eff
+           "euler_rel_err": abs(float((s.kappa.double() * g).sum()) - float(s.D_eff[0])) / float(s.D_eff[0])}
+    if fd_voxels:
+        def deff(kk):
+            t = tg.KappaSolver(kk, device=dev)
+            t.warm_start(s)
+            t.solve(conv_crit=1e-3, refine={"tol": fd_tol})
+            return t.D_eff[0]
+
+        rng = np.random.default_rng(3004)
+        gn = g[0].cpu().numpy()
+        errs = []
+        for _ in range(fd_voxels):
+            i = tuple(int(rng.integers(0, side)) for _ in range(3))
+            kp, km = kap.copy(), kap.copy()
+            kp[i] += np.float32(1e-3)
+            km[i] -= np.float32(1e-3)
+            fd = (deff(kp) - deff(km)) / (float(kp[i]) - float(km[i]))
+            errs.append(abs(fd - gn[i]) / abs(fd))
+        out["fd_h"] = 1e-3
+        out["fd_voxels"] = fd_voxels
+        out["fd_max_rel_err"] = float(max(errs))
+        out["fd_median_rel_err"] = float(np.median(errs))
+        # directional derivative along a random +-1 pattern over all voxels (strong signal)
+        v = np.where(rng.random(kap.shape) < 0.5, -1.0, 1.0).astype(np.float32)
+        kp = (kap + np.float32(1e-3) * v).astype(np.float32)
+        km = (kap - np.float32(1e-3) * v).astype(np.float32)
+        fd = (deff(kp) - deff(km)) / 2.0
+        step = (kp.astype(np.float64) - km.astype(np.float64)) / 2.0
+        out["fd_direction_rel_err"] = float(abs(fd - float((gn * step).sum())) / abs(fd))
+    return out
+
+
 def run_profile(args):
     """Small fixed workload for profiler captures: `--half-sweeps` half-sweeps of a
     `--batch` x `--side`^3 batch after 8 warm-up half-sweeps. Prints nothing to measure."""
@@ -327,8 +432,20 @@ def main():
     ap.add_argument("--side", type=int, default=256, help="--profile: volume side")
     ap.add_argument("--half-sweeps", type=int, default=40, help="--profile: half-sweeps")
     ap.add_argument("--periodic", action="store_true", help="--profile: PeriodicSolver")
+    ap.add_argument("--workload", choices=["uneven", "adjoint"], default=None,
+                    help="print the secondary measurement of this workload only")
+    ap.add_argument("--fd-voxels", type=int, default=0, help="--workload adjoint: finite-difference check")
+    ap.add_argument("--adj-side", dest="adj_side", type=int, default=320, help="--workload adjoint: volume side")
     args = ap.parse_args()
-    if args.profile:
+    if args.workload:
+        import torch
+
+        dev = torch.device("cuda", 0)
+        if args.workload == "uneven":
+            print(json.dumps(uneven_batch(dev)), flush=True)
+        else:
+            print(json.dumps(adjoint_cost(dev, args.adj_side, args.fd_voxels)), flush=True)
+    elif args.profile:
         run_profile(args)
     elif args.impl == "reference":
         run_reference(args)

@@ -256,22 +256,27 @@ int tf_kappa_pack(const tf_geom* g, const tf_operator* op, const float* kappa_de
 int tf_kappa_advance(const tf_geom* g, const tf_operator* op, float* field_dev, const float* kappa_split_dev,
                      const float* rhs_dev, int first_colour, int n_half, void* stream);
 
+/* Coefficients of the float64 steps below (coeff_f64): 0 = the sweeps' own float32 faces and
+ * float32 diagonal (the reference's discrete operator, taufactor.py:577-603); 1 = float64 faces
+ * 2ab/(a+b) of the float32 kappa values and the exact float64 diagonal, under which D_eff is a
+ * smooth function of kappa (the form that gradients and their finite-difference checks need). */
+
 /* per-plane float64 sums of face * (c[x+1] - c[x]) and of c (taufactor.py:615-620, :296, :307);
- * field_dev is float (field_is_f64 = 0) or double (1). */
-int tf_kappa_layer_sums(const tf_geom* g, const void* field_dev, int field_is_f64, const float* kappa_split_dev,
-                        double* flux_sum_dev, double* c_sum_dev, void* stream);
+ * field_dev is float (field_is_f64 = 0, float32 faces; coeff_f64 must be 0) or double (1). */
+int tf_kappa_layer_sums(const tf_geom* g, const void* field_dev, int field_is_f64, int coeff_f64,
+                        const float* kappa_split_dev, double* flux_sum_dev, double* c_sum_dev, void* stream);
 
 /* float64 residual r = b - A c; b = the Dirichlet terms of op (b64_dev NULL) or b64_dev
  * (double [field_elems]). r -> rhs_dev (float, periodic ghosts rebuilt); per-plane sums of r^2
  * and b^2 -> r2_sum_dev / b2_sum_dev [batch][nx]. */
 int tf_kappa_residual_f64(const tf_geom* g, const tf_operator* op, const double* field64_dev,
-                          const float* kappa_split_dev, const double* b64_dev, float* rhs_dev, double* r2_sum_dev,
-                          double* b2_sum_dev, void* stream);
+                          const float* kappa_split_dev, const double* b64_dev, int coeff_f64, float* rhs_dev,
+                          double* r2_sum_dev, double* b2_sum_dev, void* stream);
 
 /* Adjoint right-hand side dD_eff/dc = scale * (face_{x-1|x} - face_{x|x+1}) per voxel
  * (double [field_elems]); scale = D_0 nx / (|bc_hi - bc_lo| (nx-1) ny nz). */
 int tf_kappa_adjoint_rhs(const tf_geom* g, const float* kappa_split_dev, double* out64_dev, double scale,
-                         void* stream);
+                         int coeff_f64, void* stream);
 
 /* dD_eff/dkappa per voxel, double [batch][nx][ny][nz], from the float64 field c and the adjoint
  * lambda (A lambda = dD_eff/dc): interior faces -(lam_u - lam_w)(c_u - c_w) (+ scale *

@@ -17,6 +17,10 @@ converges to (tldr-group/taufactor v1.2.1, taufactor/taufactor.py):
   divisor ``factor`` (nn or the float32 sum of faces), so the FP64 solution is the fixed point of
   the reference's own discrete operator.
 
+For the per-voxel conductivity kinds ('kappa', 'periodic_kappa') ``coefficients="f64"`` takes
+instead float64 faces 2ab/(a+b) of the float32 kappa values and the exact float64 diagonal: the
+smooth operator whose D_eff the product differentiates (its ``KappaSolver`` default).
+
 Voxels of clusters that touch neither Dirichlet face make the operator singular; they carry no
 flux at convergence, so they are removed (pinned to 0). The system is solved with
 Jacobi-preconditioned CG to a relative residual of 1e-10, and D_eff is formed with the
@@ -32,13 +36,40 @@ from scipy.sparse.linalg import cg
 from .sor import OracleSolve
 
 
-def _face_weights(o: OracleSolve):
+def _hm64(a, b):
+    """float64 harmonic face 2ab/(a+b), 0 where a + b == 0."""
+    s_ = a + b
+    return np.where(s_ > 0, 2.0 * a * b / np.where(s_ > 0, s_, 1.0), 0.0)
+
+
+def _exact(o: OracleSolve, coefficients: str) -> bool:
+    if coefficients not in ("f32", "f64"):
+        raise ValueError(coefficients)
+    if coefficients == "f64" and not hasattr(o, "kappa"):
+        raise ValueError('coefficients="f64" applies to the kappa kinds only')
+    return coefficients == "f64"
+
+
+def _face_weights(o: OracleSolve, coefficients: str = "f32"):
     """Conductances of the +x, +y, +z faces of every voxel, [B,X,Y,Z] float64 each.
 
     The last y/z face wraps to index 0 for periodic solvers and is 0 otherwise; the last x
     face (outlet) is handled as a Dirichlet term, so its entry here is 0.
     """
     B, X, Y, Z = o.batch_size, o.Nx, o.Ny, o.Nz
+    if _exact(o, coefficients):
+        k = o.kappa.astype(np.float64)
+        gx = np.zeros((B, X, Y, Z))
+        gx[:, :-1] = _hm64(k[:, :-1], k[:, 1:])
+        if o.periodic:
+            gy = _hm64(k, np.roll(k, -1, axis=2))
+            gz = _hm64(k, np.roll(k, -1, axis=3))
+        else:
+            gy = np.zeros((B, X, Y, Z))
+            gy[:, :, :-1] = _hm64(k[:, :, :-1], k[:, :, 1:])
+            gz = np.zeros((B, X, Y, Z))
+            gz[:, :, :, :-1] = _hm64(k[:, :, :, :-1], k[:, :, :, 1:])
+        return gx, gy, gz, k[:, 0], k[:, -1]
     if o.multiphase:
         gx = np.zeros((B, X, Y, Z))
         gx[:, :-1] = o.D_x[:, 1:-1]
@@ -69,10 +100,10 @@ def _face_weights(o: OracleSolve):
     return gx, gy, gz, m[:, 0], m[:, -1]
 
 
-def assemble(o: OracleSolve, b: int):
+def assemble(o: OracleSolve, b: int, coefficients: str = "f32"):
     """Sparse SPD system (A, rhs, index map) of batch element b."""
     X, Y, Z = o.Nx, o.Ny, o.Nz
-    gx, gy, gz, gb_lo, gb_hi = (a[b] for a in _face_weights(o))
+    gx, gy, gz, gb_lo, gb_hi = (a[b] for a in _face_weights(o, coefficients))
     n = X * Y * Z
     idx = np.arange(n).reshape(X, Y, Z)
     rows, cols, vals = [], [], []
@@ -106,21 +137,22 @@ def assemble(o: OracleSolve, b: int):
     anchored[comp[dirichlet]] = True
     keep = active & anchored[comp]
     # the reference's float32 divisor (finite where the voxel is updated)
-    fac = o.factor[b].astype(np.float64).ravel()
-    diag = np.where(np.isfinite(fac) & (diag > 0), fac, diag)
+    if not _exact(o, coefficients):
+        fac = o.factor[b].astype(np.float64).ravel()
+        diag = np.where(np.isfinite(fac) & (diag > 0), fac, diag)
     A = (off + sp.diags(diag)).tocsr()
     k = np.nonzero(keep)[0]
     return A[k][:, k].tocsr(), rhs[k], k
 
 
-def solve_fp64(o: OracleSolve, rtol: float = 1e-10, maxiter: int = 200000):
+def solve_fp64(o: OracleSolve, rtol: float = 1e-10, maxiter: int = 200000, coefficients: str = "f32"):
     """FP64 field [B,X,Y,Z] (0 outside anchored clusters) and the CG residuals reached."""
     B, X, Y, Z = o.batch_size, o.Nx, o.Ny, o.Nz
     field = np.zeros((B, X, Y, Z))
     resid = np.zeros(B)
     prof = np.linspace(o.top_bc + 0.5 / X, o.bot_bc - 0.5 / X, X)
     for b in range(B):
-        A, rhs, k = assemble(o, b)
+        A, rhs, k = assemble(o, b, coefficients)
         if len(k) == 0:
             continue
         x0 = np.broadcast_to(prof[:, None, None], (X, Y, Z)).ravel()[k]
@@ -136,9 +168,12 @@ def solve_fp64(o: OracleSolve, rtol: float = 1e-10, maxiter: int = 200000):
     return field, resid
 
 
-def layer_flux_fp64(o: OracleSolve, field: np.ndarray) -> np.ndarray:
+def layer_flux_fp64(o: OracleSolve, field: np.ndarray, coefficients: str = "f32") -> np.ndarray:
     """Reference layer-flux formula (taufactor.py:412-419, :615-620) in float64, [B,X-1]."""
     d = field[:, 1:] - field[:, :-1]
+    if _exact(o, coefficients):
+        k = o.kappa.astype(np.float64)
+        return (_hm64(k[:, :-1], k[:, 1:]) * d).mean(axis=(2, 3))
     if o.multiphase:
         return (o.D_x[:, 1:-1].astype(np.float64) * d).mean(axis=(2, 3))
     # Solver.vertical_flux zeroes faces whose divisor exceeds 8 (:417-418; for the anisotropic
@@ -148,15 +183,15 @@ def layer_flux_fp64(o: OracleSolve, field: np.ndarray) -> np.ndarray:
     return d.mean(axis=(2, 3))
 
 
-def d_eff_fp64(o: OracleSolve, rtol: float = 1e-10):
+def d_eff_fp64(o: OracleSolve, rtol: float = 1e-10, coefficients: str = "f32"):
     """FP64 D_eff per batch element (D_0 * mean layer flux * Nx / |bc difference|)."""
-    field, resid = solve_fp64(o, rtol=rtol)
-    flux = layer_flux_fp64(o, field)
+    field, resid = solve_fp64(o, rtol=rtol, coefficients=coefficients)
+    flux = layer_flux_fp64(o, field, coefficients)
     d_rel = flux.mean(axis=1) * o.Nx / abs(o.top_bc - o.bot_bc)
     return o.D_0 * d_rel, field, resid
 
 
-def adjoint_gradient_fp64(o: OracleSolve, rtol: float = 1e-12):
+def adjoint_gradient_fp64(o: OracleSolve, rtol: float = 1e-12, coefficients: str = "f32"):
     """FP64 dD_eff/dkappa [B,X,Y,Z] of a per-voxel conductivity field (kind 'kappa' /
     'periodic_kappa'), by the adjoint method on the operator assembled above.
 
@@ -168,16 +203,19 @@ def adjoint_gradient_fp64(o: OracleSolve, rtol: float = 1e-12):
     """
     B, X, Y, Z = o.batch_size, o.Nx, o.Ny, o.Nz
     K = o.D_0 * X / (abs(o.top_bc - o.bot_bc) * (X - 1) * Y * Z)
-    field, _ = solve_fp64(o, rtol=rtol)
+    field, _ = solve_fp64(o, rtol=rtol, coefficients=coefficients)
     grads = np.zeros((B, X, Y, Z))
+    exact = _exact(o, coefficients)
 
     def dface(a, w):
         s_ = a + w
         return np.where(s_ > 0, 2 * w * w / np.where(s_ > 0, s_ * s_, 1.0), 0.0)
 
     for b in range(B):
-        A, _, keep = assemble(o, b)
-        gx = o.D_x[b, 1:-1].astype(np.float64)  # faces between planes x and x+1
+        A, _, keep = assemble(o, b, coefficients)
+        k64 = o.kappa[b].astype(np.float64)
+        # faces between planes x and x+1
+        gx = _hm64(k64[:-1], k64[1:]) if exact else o.D_x[b, 1:-1].astype(np.float64)
         dj = np.zeros((X, Y, Z))
         dj[1:] += gx
         dj[:-1] -= gx

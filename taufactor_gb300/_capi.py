@@ -102,9 +102,9 @@ def load():
         "tf_batch_converge_static": (i32, [vp, vp, i32, i32, i64, i64, TfBatchState, C.c_double, i32, i32, vp]),
         "tf_kappa_pack": (i32, [G, O, vp, vp, vp, vp, vp]),
         "tf_kappa_advance": (i32, [G, O, vp, vp, vp, i32, i32, vp]),
-        "tf_kappa_layer_sums": (i32, [G, vp, i32, vp, vp, vp, vp]),
-        "tf_kappa_residual_f64": (i32, [G, O, vp, vp, vp, vp, vp, vp, vp]),
-        "tf_kappa_adjoint_rhs": (i32, [G, vp, vp, C.c_double, vp]),
+        "tf_kappa_layer_sums": (i32, [G, vp, i32, i32, vp, vp, vp, vp]),
+        "tf_kappa_residual_f64": (i32, [G, O, vp, vp, vp, i32, vp, vp, vp, vp]),
+        "tf_kappa_adjoint_rhs": (i32, [G, vp, vp, C.c_double, i32, vp]),
         "tf_kappa_gradient": (i32, [G, O, vp, vp, vp, vp, C.c_double, C.c_double, C.c_double, vp]),
         "tf_split_to_natural_f64": (i32, [G, vp, vp, vp]),
     }

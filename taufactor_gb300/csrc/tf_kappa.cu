@@ -10,6 +10,13 @@
 // k_kappa_sweep      one half-sweep in place (float4 groups of one colour), optional RHS
 // k_kappa_residual   float64 r = b - A c with an explicit float64 right-hand side or the
 //                    Dirichlet terms; per-plane sums of r^2 and b^2
+//
+// The float64 steps (residual, float64 layer sums, adjoint right-hand side) take their
+// coefficients either as the sweeps do (float32 faces and float32 `factor`: the reference's own
+// discrete operator) or as float64 faces 2ab/(a+b) of the float32 kappa values with the exact
+// float64 diagonal. In the second form D_eff is a smooth function of kappa, which is what
+// dD_eff/dkappa and its finite-difference checks need: float32 faces change in steps of one
+// rounding, so a central difference of step h carries noise of about 1e-7/h relative.
 // k_kappa_layer_sums per-plane float64 sums of face_x * (c[x+1] - c[x]) and of c
 // k_kappa_dJdc       adjoint right-hand side dD_eff/dc (float64)
 // k_kappa_grad       dD_eff/dkappa per voxel from c and the adjoint lambda (float64)
@@ -59,6 +66,48 @@ __device__ __forceinline__ Faces kappa_faces(const float* kp, const KView& v, in
     return f;
 }
 
+// float64 face of the float32 values a, b: 2ab/(a+b), 0 when a + b == 0 (hface64(k, k) = k)
+__device__ __forceinline__ double hface64(double a, double b) {
+    const double den = a + b;
+    return den > 0.0 ? 2.0 * a * b / den : 0.0;
+}
+
+// The faces and the diagonal in float64; F64C selects float64 coefficients, otherwise the
+// float32 ones of kappa_faces widened. `active` = the voxel has a finite diagonal.
+struct Faces64 {
+    double xp, xm, yp, ym, zp, zm, div;
+    bool active;
+};
+
+template <bool F64C>
+__device__ __forceinline__ Faces64 kappa_faces_fp64(const float* kp, const KView& v, int x, int y, int z, float kc) {
+    Faces64 d;
+    if (F64C) {
+        const double k = kc;
+        d.xm = x > 0 ? hface64(k, kp[v.off(x - 1, y, z)]) : k;
+        d.xp = x + 1 < v.g.NX ? hface64(k, kp[v.off(x + 1, y, z)]) : k;
+        d.ym = hface64(k, kp[v.off(x, y - 1, z)]);
+        d.yp = hface64(k, kp[v.off(x, y + 1, z)]);
+        d.zm = hface64(k, kp[v.off(x, y, z - 1)]);
+        d.zp = hface64(k, kp[v.off(x, y, z + 1)]);
+        d.div = d.xm + d.xp + d.ym + d.yp + d.zm + d.zp;
+        if (x == 0) d.div += d.xm;
+        if (x == v.g.NX - 1) d.div += d.xp;
+        d.active = d.div > 0.0;
+    } else {
+        const Faces f = kappa_faces(kp, v, x, y, z, kc);
+        d.xm = f.xm;
+        d.xp = f.xp;
+        d.ym = f.ym;
+        d.yp = f.yp;
+        d.zm = f.zm;
+        d.zp = f.zp;
+        d.div = f.div;
+        d.active = f.div < __int_as_float(0x7f800000);
+    }
+    return d;
+}
+
 // One thread per interior voxel of colour `colour`; in place (neighbours have the other colour,
 // and periodic ghosts are refreshed after the launch, as for the plain binary sweep).
 __global__ void __launch_bounds__(256) k_kappa_sweep(float* __restrict__ c, const float* __restrict__ kp,
@@ -94,6 +143,7 @@ __global__ void __launch_bounds__(256) k_kappa_sweep(float* __restrict__ c, cons
 }
 
 // float64 residual; bsrc (float64, split layout) replaces the Dirichlet terms when non-null.
+template <bool F64C>
 __global__ void __launch_bounds__(256) k_kappa_residual(const double* __restrict__ c64, const float* __restrict__ kp,
                                                         const double* __restrict__ bsrc, float* __restrict__ r32,
                                                         double* __restrict__ r2, double* __restrict__ b2, const Geo g,
@@ -108,17 +158,17 @@ __global__ void __launch_bounds__(256) k_kappa_residual(const double* __restrict
     for (long long it = threadIdx.x; it < (long long)g.NY * g.NZ; it += blockDim.x) {
         const int y = (int)(it / g.NZ), z = (int)(it - (long long)y * g.NZ);
         const long long o = v.off(x, y, z);
-        const Faces f = kappa_faces(kb, v, x, y, z, kb[o]);
+        const Faces64 f = kappa_faces_fp64<F64C>(kb, v, x, y, z, kb[o]);
         double res = 0.0, rhs = 0.0;
-        if (f.div < __int_as_float(0x7f800000)) {
-            double s = (double)f.yp * cb[v.off(x, y + 1, z)] + (double)f.ym * cb[v.off(x, y - 1, z)] +
-                       (double)f.zp * cb[v.off(x, y, z + 1)] + (double)f.zm * cb[v.off(x, y, z - 1)];
-            if (x > 0) s += (double)f.xm * cb[v.off(x - 1, y, z)];
-            else if (!bsrc) rhs += (double)f.xm * glo;
-            if (x + 1 < g.NX) s += (double)f.xp * cb[v.off(x + 1, y, z)];
-            else if (!bsrc) rhs += (double)f.xp * ghi;
+        if (f.active) {
+            double s = f.yp * cb[v.off(x, y + 1, z)] + f.ym * cb[v.off(x, y - 1, z)] +
+                       f.zp * cb[v.off(x, y, z + 1)] + f.zm * cb[v.off(x, y, z - 1)];
+            if (x > 0) s += f.xm * cb[v.off(x - 1, y, z)];
+            else if (!bsrc) rhs += f.xm * glo;
+            if (x + 1 < g.NX) s += f.xp * cb[v.off(x + 1, y, z)];
+            else if (!bsrc) rhs += f.xp * ghi;
             if (bsrc) rhs = bsrc[b0 + o];
-            res = rhs - ((double)f.div * cb[o] - s);
+            res = rhs - (f.div * cb[o] - s);
         }
         r32[b0 + o] = (float)res;
         rs += res * res;
@@ -144,8 +194,8 @@ __global__ void __launch_bounds__(256) k_kappa_residual(const double* __restrict
     }
 }
 
-// T = float or double field
-template <typename T>
+// T = float or double field; F64C (double fields only) = float64 faces
+template <typename T, bool F64C>
 __global__ void __launch_bounds__(256) k_kappa_layer_sums(const T* __restrict__ c, const float* __restrict__ kp,
                                                           double* __restrict__ flux, double* __restrict__ csum,
                                                           const Geo g) {
@@ -162,11 +212,13 @@ __global__ void __launch_bounds__(256) k_kappa_layer_sums(const T* __restrict__ 
         cs += (double)a;
         if (has_flux) {
             const long long o1 = v.off(x + 1, y, z);
-            const float face = hface(kp[b0 + o], kp[b0 + o1]);
-            if (sizeof(T) == 4)
+            if (sizeof(T) == 4) {
+                const float face = hface(kp[b0 + o], kp[b0 + o1]);
                 fs += (double)__fmul_rn(face, __fsub_rn((float)c[b0 + o1], (float)a));  // :617-619 in float32
-            else
-                fs += (double)face * ((double)c[b0 + o1] - (double)a);
+            } else {
+                const double face = F64C ? hface64(kp[b0 + o], kp[b0 + o1]) : (double)hface(kp[b0 + o], kp[b0 + o1]);
+                fs += face * ((double)c[b0 + o1] - (double)a);
+            }
         }
     }
     for (int s = 16; s > 0; s >>= 1) {
@@ -192,6 +244,7 @@ __global__ void __launch_bounds__(256) k_kappa_layer_sums(const T* __restrict__ 
 // dJ/dc for J = D_0 * mean_x(layer flux) * Nx / |bc_hi - bc_lo| with layer flux
 // (1/(Ny Nz)) sum face_x (c[x+1] - c[x]): dJ/dc[x] = K (face_{x-1|x} - face_{x|x+1}),
 // K = D_0 Nx / (|dbc| (Nx-1) Ny Nz). Written for interior voxels (0 elsewhere).
+template <bool F64C>
 __global__ void k_kappa_dJdc(const float* __restrict__ kp, double* __restrict__ g_out, const Geo g, double K) {
     const KView v{g};
     const long long n = (long long)g.NX * g.NY * g.NZ;
@@ -204,8 +257,14 @@ __global__ void k_kappa_dJdc(const float* __restrict__ kp, double* __restrict__ 
     const long long o = v.off(x, y, z);
     const float kc = kp[b0 + o];
     double d = 0.0;
-    if (x > 0) d += (double)hface(kp[b0 + v.off(x - 1, y, z)], kc);
-    if (x + 1 < g.NX) d -= (double)hface(kc, kp[b0 + v.off(x + 1, y, z)]);
+    if (x > 0) {
+        const float kw = kp[b0 + v.off(x - 1, y, z)];
+        d += F64C ? hface64(kw, kc) : (double)hface(kw, kc);
+    }
+    if (x + 1 < g.NX) {
+        const float kw = kp[b0 + v.off(x + 1, y, z)];
+        d -= F64C ? hface64(kc, kw) : (double)hface(kc, kw);
+    }
     g_out[b0 + o] = K * d;
 }
 
@@ -357,40 +416,52 @@ int tf_kappa_advance(const tf_geom* g, const tf_operator* op, float* field_dev, 
     return TF_OK;
 }
 
-int tf_kappa_layer_sums(const tf_geom* g, const void* field_dev, int field_is_f64, const float* kappa_split_dev,
-                        double* flux_sum_dev, double* c_sum_dev, void* stream) {
+int tf_kappa_layer_sums(const tf_geom* g, const void* field_dev, int field_is_f64, int coeff_f64,
+                        const float* kappa_split_dev, double* flux_sum_dev, double* c_sum_dev, void* stream) {
     if (!g || !field_dev || !kappa_split_dev || !c_sum_dev || (g->nx > 1 && !flux_sum_dev)) return TF_ERR_ARG;
+    if (coeff_f64 && !field_is_f64) return TF_ERR_ARG;
     const Geo geo = make_geo(*g);
     dim3 grid(g->nx, g->batch);
-    if (field_is_f64)
-        k_kappa_layer_sums<double><<<grid, 256, 0, (cudaStream_t)stream>>>(
+    if (field_is_f64 && coeff_f64)
+        k_kappa_layer_sums<double, true><<<grid, 256, 0, (cudaStream_t)stream>>>(
+            static_cast<const double*>(field_dev), kappa_split_dev, flux_sum_dev, c_sum_dev, geo);
+    else if (field_is_f64)
+        k_kappa_layer_sums<double, false><<<grid, 256, 0, (cudaStream_t)stream>>>(
             static_cast<const double*>(field_dev), kappa_split_dev, flux_sum_dev, c_sum_dev, geo);
     else
-        k_kappa_layer_sums<float><<<grid, 256, 0, (cudaStream_t)stream>>>(
+        k_kappa_layer_sums<float, false><<<grid, 256, 0, (cudaStream_t)stream>>>(
             static_cast<const float*>(field_dev), kappa_split_dev, flux_sum_dev, c_sum_dev, geo);
     note_launch();
     return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
 }
 
 int tf_kappa_residual_f64(const tf_geom* g, const tf_operator* op, const double* field64_dev,
-                          const float* kappa_split_dev, const double* b64_dev, float* rhs_dev, double* r2_sum_dev,
-                          double* b2_sum_dev, void* stream) {
+                          const float* kappa_split_dev, const double* b64_dev, int coeff_f64, float* rhs_dev,
+                          double* r2_sum_dev, double* b2_sum_dev, void* stream) {
     if (!g || !op || !field64_dev || !kappa_split_dev || !rhs_dev || !r2_sum_dev || !b2_sum_dev) return TF_ERR_ARG;
     const Geo geo = make_geo(*g);
-    k_kappa_residual<<<dim3(g->nx, g->batch), 256, 0, (cudaStream_t)stream>>>(
-        field64_dev, kappa_split_dev, b64_dev, rhs_dev, r2_sum_dev, b2_sum_dev, geo, op->ghost_lo, op->ghost_hi);
+    const dim3 grid(g->nx, g->batch);
+    if (coeff_f64)
+        k_kappa_residual<true><<<grid, 256, 0, (cudaStream_t)stream>>>(
+            field64_dev, kappa_split_dev, b64_dev, rhs_dev, r2_sum_dev, b2_sum_dev, geo, op->ghost_lo, op->ghost_hi);
+    else
+        k_kappa_residual<false><<<grid, 256, 0, (cudaStream_t)stream>>>(
+            field64_dev, kappa_split_dev, b64_dev, rhs_dev, r2_sum_dev, b2_sum_dev, geo, op->ghost_lo, op->ghost_hi);
     note_launch();
     if (cudaGetLastError() != cudaSuccess) return TF_ERR_CUDA;
     return op->periodic ? refresh_ghosts(*g, op->periodic, rhs_dev, (cudaStream_t)stream) : TF_OK;
 }
 
 int tf_kappa_adjoint_rhs(const tf_geom* g, const float* kappa_split_dev, double* out64_dev, double scale,
-                         void* stream) {
+                         int coeff_f64, void* stream) {
     if (!g || !kappa_split_dev || !out64_dev) return TF_ERR_ARG;
     const Geo geo = make_geo(*g);
     const long long n = (long long)g->nx * g->ny * g->nz;
-    k_kappa_dJdc<<<dim3((unsigned)((n + 255) / 256), g->batch), 256, 0, (cudaStream_t)stream>>>(kappa_split_dev,
-                                                                                                out64_dev, geo, scale);
+    const dim3 grid((unsigned)((n + 255) / 256), g->batch);
+    if (coeff_f64)
+        k_kappa_dJdc<true><<<grid, 256, 0, (cudaStream_t)stream>>>(kappa_split_dev, out64_dev, geo, scale);
+    else
+        k_kappa_dJdc<false><<<grid, 256, 0, (cudaStream_t)stream>>>(kappa_split_dev, out64_dev, geo, scale);
     note_launch();
     return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
 }

@@ -88,3 +88,29 @@ def test_percolation_restatement():
     assert not spans_axis0(m)
     m[2:5, 2, 3] = True  # detour around the gap
     assert spans_axis0(m)
+
+
+@pytest.mark.parametrize("coefficients", ["f32", "f64"])
+def test_fp64_adjoint_gradient_euler_and_finite_differences(coefficients):
+    """The FP64 adjoint gradient of a per-voxel conductivity field: Euler's identity
+    sum(kappa dD/dkappa) = D_eff (D_eff is homogeneous of degree 1 in kappa) and central
+    finite differences (h = 1e-3). With float32 faces D_eff moves in steps of one face rounding,
+    so the finite differences only hold to ~1e-3; with float64 faces to the h^2 truncation."""
+    from oracle.fp64 import adjoint_gradient_fp64
+
+    kap = (0.05 + np.random.default_rng(71).random((1, 10, 9, 12))).astype(np.float32)
+    o = OracleSolve(kap, kind="kappa")
+    g = adjoint_gradient_fp64(o, rtol=1e-14, coefficients=coefficients)[0]
+    d = d_eff_fp64(o, rtol=1e-14, coefficients=coefficients)[0][0]
+    euler = abs(float((kap[0].astype(np.float64) * g).sum()) - d) / d
+    assert euler < (1e-13 if coefficients == "f64" else 1e-8), euler
+    rng = np.random.default_rng(72)
+    for _ in range(3):
+        i = tuple(int(rng.integers(0, n)) for n in kap.shape[1:])
+        kp, km = kap.copy(), kap.copy()
+        kp[(0,) + i] += np.float32(1e-3)
+        km[(0,) + i] -= np.float32(1e-3)
+        dp = d_eff_fp64(OracleSolve(kp, kind="kappa"), rtol=1e-14, coefficients=coefficients)[0][0]
+        dm = d_eff_fp64(OracleSolve(km, kind="kappa"), rtol=1e-14, coefficients=coefficients)[0][0]
+        fd = (dp - dm) / (float(kp[(0,) + i]) - float(km[(0,) + i]))
+        assert abs(fd - g[i]) / abs(fd) < (1e-5 if coefficients == "f64" else 3e-3), (i, fd, g[i])
