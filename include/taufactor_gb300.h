@@ -204,6 +204,19 @@ int tf_batch_describe(int n_vol, const tf_geom* geoms, const tf_operator* ops, f
                       float* const* field_b, const uint8_t* const* codes, const int64_t* flux_off,
                       const int64_t* csum_off, const double* d_mean, int32_t* err_dev, void* desc_dev);
 
+/* Descriptor table for batched FP64 defect correction (no reference counterpart): the sweeps
+ * solve A e = r per volume with Dirichlet ghosts 0, rhs[v] = float32 right-hand side of volume v
+ * (16-byte aligned, field layout), e ping-ponging between field_a[v] and field_b[v]. Synchronous. */
+int tf_batch_describe_rhs(int n_vol, const tf_geom* geoms, const tf_operator* ops, float* const* field_a,
+                          float* const* field_b, const uint8_t* const* codes, const float* const* rhs,
+                          int32_t* err_dev, void* desc_dev);
+
+/* Launch number `launch` (0, 1, ...) of a batched correction solve on a tf_batch_describe_rhs
+ * table: volume v takes part while launch < launches_dev[v] (int32 per volume; give an even
+ * count so that its result ends in field A). Launch parity selects A -> B or B -> A. */
+int tf_batch_advance_rhs(const void* desc_dev, const int32_t* work_dev, int n_work, const int32_t* launches_dev,
+                         int launch, void* stream);
+
 /* Advance every active volume by the batch's half-sweeps per launch (colour 0 first, so the
  * completed half-sweeps must stay a multiple of it). work_dev: int32 pairs (volume, tile) with
  * tile = ty * tiles_z + tz. parity 0 reads buffers A and writes B, 1 the reverse. */

@@ -22,6 +22,7 @@ EXPORTS = (
     "tf_layer_sums", "tf_unpack", "tf_repack", "tf_check_small_division", "tf_advance_rhs", "tf_widen_f64",
     "tf_narrow_f64", "tf_axpy_f64", "tf_residual_f64", "tf_layer_sums_f64", "tf_batch_desc_bytes", "tf_batch_tile",
     "tf_batch_describe", "tf_batch_advance", "tf_batch_layer_sums", "tf_batch_check", "tf_batch_tick",
+    "tf_batch_describe_rhs", "tf_batch_advance_rhs",
     "tf_batch_converge_static", "tf_kappa_pack", "tf_kappa_advance", "tf_kappa_layer_sums",
     "tf_kappa_residual_f64", "tf_kappa_adjoint_rhs", "tf_kappa_gradient", "tf_split_to_natural_f64",
 )
@@ -96,6 +97,8 @@ def load():
         "tf_batch_tile": (None, [C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
         "tf_batch_describe": (i32, [i32, G, O, vp, vp, vp, vp, vp, vp, vp, vp]),
         "tf_batch_advance": (i32, [vp, vp, i32, vp, i32, vp]),
+        "tf_batch_describe_rhs": (i32, [i32, G, O, vp, vp, vp, vp, vp, vp]),
+        "tf_batch_advance_rhs": (i32, [vp, vp, i32, vp, i32, vp]),
         "tf_batch_layer_sums": (i32, [vp, vp, i32, vp, i32, vp, vp, vp]),
         "tf_batch_check": (i32, [vp, i32, vp, TfBatchState, C.c_double, i32, i32, vp]),
         "tf_batch_tick": (i32, [vp, i32, vp]),

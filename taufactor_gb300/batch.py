@@ -15,7 +15,8 @@ volume keeps its own shape, buffers and convergence state:
 
 Each volume's result equals what ``Solver`` / ``PeriodicSolver`` return for it alone, except
 that a volume paused for the percolation test skips one tau update. Optional FP64 defect
-correction (``refine=True``) follows per volume.
+correction (``refine=True``) then runs for all volumes together: shared launches of the
+correction sweeps, each volume stopping at its own tolerance.
 """
 from __future__ import annotations
 
@@ -30,7 +31,7 @@ from . import _capi
 from ._capi import (TF_BATCH_ACTIVE, TF_BATCH_CONVERGED, TF_BATCH_NEEDS_HOST, TF_KIND_BINARY, TF_PERIODIC_Y,
                     TF_PERIODIC_Z, TfBatchState, TfGeom, TfOperator, check)
 from .percolation import spans_x
-from .solvers import layer_metrics, refine_field
+from .solvers import layer_metrics
 
 INTERVAL = 100  # half-sweeps between convergence checks (taufactor.py:184-185)
 
@@ -167,6 +168,8 @@ class BatchSolve:
         self.iter_offset = np.zeros(n, dtype=np.int64)
         self._final_in_b = np.zeros(n, dtype=bool)
         self.graph = None
+        self._rhs = None
+        self.c64 = None
         self.walltime = 0.0
 
     def _stream(self):
@@ -233,6 +236,7 @@ class BatchSolve:
         """
         limit = (iter_limit // (2 * INTERVAL)) * 2 * INTERVAL
         start = timer()
+        self.c64 = None
         with torch.cuda.device(self.device):
             if graph and self.graph is None:
                 self.graph = self._capture(conv_crit)
@@ -296,21 +300,89 @@ class BatchSolve:
                                      self._stream()), "tf_unpack")
         return out
 
-    def refine(self, tol: float = 1e-10, max_outer: int = 12):
-        """FP64 defect correction of every volume's converged field (see SORSolver.refine)."""
-        lib = self.lib
-        for v, res in enumerate(self.results):
-            cur = self.fb[v] if self._final_in_b[v] else self.fa[v]
-            g, op = self.geoms[v], self.ops[v]
-            c64, hist = refine_field(lib, g, op, cur, self.codes[v], self.err, self._stream(), 1, tol, max_outer,
-                                     max(400, 2 * res.iter))
-            flux = torch.empty(max(res.Nx - 1, 1), dtype=torch.float64, device=self.device)
-            csum = torch.empty(res.Nx, dtype=torch.float64, device=self.device)
-            check(lib.tf_layer_sums_f64(C.byref(g), C.byref(op), _ptr(c64), _ptr(self.codes[v]), _ptr(flux),
-                                        _ptr(csum), self._stream()), "tf_layer_sums_f64")
-            area = float(res.Ny * res.Nz)
-            res.flux_1d = flux.cpu().numpy()[None, : res.Nx - 1] / area
-            tau, _ = layer_metrics(res, res.flux_1d, csum.cpu().numpy()[None] / area)
-            res.tau = np.where(tau == 0, np.inf, tau)
-            res.residual_history = hist
+    def refine(self, tol: float = 1e-10, max_outer: int = 24, inner_fraction: float = 0.25):
+        """FP64 defect correction of every volume's converged field, all volumes together.
+
+        Each outer step computes the float64 residual r = b - A c of every volume still above
+        `tol` (relative 2-norm), solves the correction equation A e = r in float32 for all of them
+        in shared launches (volume v runs max(100, inner_fraction * iter_v) half-sweeps, rounded
+        up to an even number of launches) and adds e to c in float64. The field buffers hold e
+        meanwhile; the rounded float64 result returns to field A. Metrics come from the float64
+        field, which a second call continues from (solve() drops it). Per volume,
+        `residual_history` lists the relative residual before every step.
+        """
+        lib, n = self.lib, self.n
+        f64 = dict(dtype=torch.float64, device=self.device)
+        with torch.cuda.device(self.device):
+            st = self._stream()
+            if self._rhs is None:
+                self._rhs = [torch.zeros(self.geoms[v].field_elems, dtype=torch.float32, device=self.device)
+                             for v in range(n)]
+                self._r2 = torch.zeros(self.csum.numel(), **f64)
+                self._b2 = torch.zeros(self.csum.numel(), **f64)
+                self.desc_rhs = torch.empty_like(self.desc)
+                P = C.c_void_p * n
+                check(lib.tf_batch_describe_rhs(n, self.geoms, self.ops, P(*[_ptr(t) for t in self.fa]),
+                                                P(*[_ptr(t) for t in self.fb]), P(*[_ptr(t) for t in self.codes]),
+                                                P(*[_ptr(t) for t in self._rhs]), _ptr(self.err),
+                                                _ptr(self.desc_rhs)), "tf_batch_describe_rhs")
+            c64 = self.c64  # a previous refinement's float64 fields, else widen the float32 ones
+            if c64 is None:
+                c64 = []
+                for v in range(n):
+                    g = self.geoms[v]
+                    cur = self.fb[v] if self._final_in_b[v] else self.fa[v]
+                    c = torch.empty(g.field_elems, **f64)
+                    check(lib.tf_widen_f64(C.byref(g), _ptr(cur), _ptr(c), st), "tf_widen_f64")
+                    c64.append(c)
+            k2 = 2 * self.k
+            want = [max(100, int(inner_fraction * max(r.iter, 1))) for r in self.results]
+            active = np.ones(n, dtype=bool)
+            hist = [[] for _ in range(n)]
+            r2o = self._r2.element_size()
+            for outer in range(max_outer + 1):
+                for v in np.nonzero(active)[0]:
+                    off = self.csum_off[v] * r2o
+                    check(lib.tf_residual_f64(C.byref(self.geoms[v]), C.byref(self.ops[v]), _ptr(c64[v]),
+                                              _ptr(self.codes[v]), _ptr(self._rhs[v]), _ptr(self._r2) + off,
+                                              _ptr(self._b2) + off, st), "tf_residual_f64")
+                r2, b2 = self._r2.cpu().numpy(), self._b2.cpu().numpy()
+                for v in np.nonzero(active)[0]:
+                    sl = slice(self.csum_off[v], self.csum_off[v] + self.results[v].Nx)
+                    rel = math.sqrt(r2[sl].sum()) / max(math.sqrt(b2[sl].sum()), 1e-300)
+                    hist[v].append(rel)
+                    if rel < tol or outer == max_outer:
+                        active[v] = False
+                if not active.any():
+                    break
+                launches = [2 * (-(-want[v] // k2)) if active[v] else 0 for v in range(n)]
+                for v in np.nonzero(active)[0]:
+                    self.fa[v].zero_()
+                self._launches = torch.tensor(launches, dtype=torch.int32).to(self.device)
+                for j in range(max(launches)):
+                    check(lib.tf_batch_advance_rhs(_ptr(self.desc_rhs), _ptr(self.work), self.n_work,
+                                                   _ptr(self._launches), j, st), "tf_batch_advance_rhs")
+                for v in np.nonzero(active)[0]:
+                    check(lib.tf_axpy_f64(C.byref(self.geoms[v]), _ptr(c64[v]), _ptr(self.fa[v]), st), "tf_axpy_f64")
+            if int(self.err.item()):
+                raise _capi.TfError(int(self.err.item()), "tf_batch_advance_rhs (device)")
+            for v in range(n):
+                g, op = self.geoms[v], self.ops[v]
+                check(lib.tf_narrow_f64(C.byref(g), C.byref(op), _ptr(c64[v]), _ptr(self.fa[v]), st), "tf_narrow_f64")
+                self._final_in_b[v] = False
+                check(lib.tf_layer_sums_f64(C.byref(g), C.byref(op), _ptr(c64[v]), _ptr(self.codes[v]),
+                                            _ptr(self.flux) + self.flux_off[v] * 8, _ptr(self.csum) + self.csum_off[v] * 8,
+                                            st), "tf_layer_sums_f64")
+            flux, csum = self.flux.cpu().numpy(), self.csum.cpu().numpy()
+            perc = self.perc.cpu().numpy()
+            for v, res in enumerate(self.results):
+                area = float(res.Ny * res.Nz)
+                res.flux_1d = flux[self.flux_off[v]:self.flux_off[v] + res.Nx - 1][None] / area
+                if perc[v] == 2:
+                    res.flux_1d = np.zeros_like(res.flux_1d)
+                c_x = csum[self.csum_off[v]:self.csum_off[v] + res.Nx][None] / area
+                tau, _ = layer_metrics(res, res.flux_1d, c_x)
+                res.tau = np.where(tau == 0, np.inf, tau)
+                res.residual_history = hist[v]
+            self.c64 = c64
         return self.results

@@ -9,6 +9,11 @@
 // k_batch_check then evaluate the reference's convergence rule (taufactor.py:109-153,
 // :293-331) per volume on the device and set its status, so a whole check interval -- sweeps,
 // layer sums, decision -- runs without the host and can be captured in a CUDA graph.
+//
+// FP64 defect correction of the whole batch uses a second table whose sweeps solve the
+// correction equation A e = r (homogeneous Dirichlet ghosts, float32 right-hand side r per
+// volume): k_stream_multi_rhs runs every volume's inner half-sweeps in the same launches, each
+// volume for its own number of launches.
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -43,6 +48,23 @@ __global__ void __launch_bounds__(BShape::NT, 2)
     const SweepArgs a = parity ? d->ba : d->ab;
     stream_tile<TF_KIND_BINARY, BTY, BTZ, BK, false>(parity ? &d->map_b : &d->map_a, &d->map_c, a, nullptr,
                                                      tz * (BTZ / 2), ty * BTY, 0, smem);
+}
+
+// Correction sweeps: launch `launch` of an inner solve; volume v takes part while
+// launch < launches[v] (an even count, so each volume's result ends in buffer A).
+__global__ void __launch_bounds__(BShape::NT, 2)
+    k_stream_multi_rhs(const VolDesc* __restrict__ desc, const int2* __restrict__ work,
+                       const int32_t* __restrict__ launches, int launch) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int2 item = work[blockIdx.x];
+    const int v = item.x;
+    if (launch >= launches[v]) return;
+    const VolDesc* d = desc + v;
+    const int tz = item.y % d->tiles_z, ty = item.y / d->tiles_z;
+    const int parity = launch & 1;
+    const SweepArgs a = parity ? d->ba : d->ab;
+    stream_tile<TF_KIND_BINARY, BTY, BTZ, BK, true>(parity ? &d->map_b : &d->map_a, &d->map_c, a, nullptr,
+                                                    tz * (BTZ / 2), ty * BTY, 0, smem);
 }
 
 // One CTA per (volume, plane): float64 sums of the masked x-flux through face x|x+1 and of the
@@ -143,17 +165,23 @@ void tf_batch_tile(int* tile_y, int* tile_z, int* half_sweeps) {
     if (half_sweeps) *half_sweeps = BK;
 }
 
-int tf_batch_describe(int n_vol, const tf_geom* geoms, const tf_operator* ops, float* const* field_a,
-                      float* const* field_b, const uint8_t* const* codes, const int64_t* flux_off,
-                      const int64_t* csum_off, const double* d_mean, int32_t* err_dev, void* desc_dev) {
-    if (n_vol <= 0 || !geoms || !ops || !field_a || !field_b || !codes || !flux_off || !csum_off || !d_mean ||
-        !desc_dev)
-        return TF_ERR_ARG;
+}  // extern "C"
+
+namespace tf {
+
+// Descriptor table of the plain solve (rhs == nullptr) or of the correction solve (rhs[v] = the
+// float32 right-hand side of volume v; Dirichlet ghosts 0; layer-sum fields unused).
+static int describe(int n_vol, const tf_geom* geoms, const tf_operator* ops, float* const* field_a,
+                    float* const* field_b, const uint8_t* const* codes, const float* const* rhs,
+                    const int64_t* flux_off, const int64_t* csum_off, const double* d_mean, int32_t* err_dev,
+                    void* desc_dev) {
     std::vector<VolDesc> h(n_vol);
     for (int v = 0; v < n_vol; ++v) {
         const tf_geom& gg = geoms[v];
-        const tf_operator& op = ops[v];
+        tf_operator op = ops[v];
         if (gg.batch != 1 || !gg.tiled || op.kind != TF_KIND_BINARY) return TF_ERR_UNSUPPORTED;
+        if (rhs && (!rhs[v] || (reinterpret_cast<uintptr_t>(rhs[v]) & 15))) return TF_ERR_ARG;
+        if (rhs) op.ghost_lo = op.ghost_hi = 0.0f;
         VolDesc& d = h[v];
         std::memset(&d, 0, sizeof(VolDesc));
         const long long planes = (long long)gg.nx;
@@ -169,21 +197,52 @@ int tf_batch_describe(int n_vol, const tf_geom* geoms, const tf_operator* ops, f
         const Geo g = make_geo(gg);
         d.ab = make_args(g, op, field_b[v], 0, BK, err_dev);
         d.ba = make_args(g, op, field_a[v], 0, BK, err_dev);
+        if (rhs) d.ab.rhs = d.ba.rhs = rhs[v];
         d.code = codes[v];
         d.tiles_z = (gg.nz + BTZ - 1) / BTZ;
         d.tiles_y = (gg.ny + BTY - 1) / BTY;
-        d.flux_off = flux_off[v];
-        d.csum_off = csum_off[v];
-        d.d_mean = d_mean[v];
+        d.flux_off = flux_off ? flux_off[v] : 0;
+        d.csum_off = csum_off ? csum_off[v] : 0;
+        d.d_mean = d_mean ? d_mean[v] : 0.0;
         d.inv_area = 1.0 / ((double)gg.ny * gg.nz);
     }
     // kernel attributes are set here, outside any stream capture
-    if (cudaFuncSetAttribute(k_stream_multi, cudaFuncAttributeMaxDynamicSharedMemorySize, BShape::SMEM) !=
-        cudaSuccess)
+    if (cudaFuncSetAttribute(rhs ? k_stream_multi_rhs : k_stream_multi, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             BShape::SMEM) != cudaSuccess)
         return TF_ERR_CUDA;
     return cudaMemcpy(desc_dev, h.data(), sizeof(VolDesc) * n_vol, cudaMemcpyHostToDevice) == cudaSuccess
                ? TF_OK
                : TF_ERR_CUDA;
+}
+
+}  // namespace tf
+
+extern "C" {
+
+int tf_batch_describe(int n_vol, const tf_geom* geoms, const tf_operator* ops, float* const* field_a,
+                      float* const* field_b, const uint8_t* const* codes, const int64_t* flux_off,
+                      const int64_t* csum_off, const double* d_mean, int32_t* err_dev, void* desc_dev) {
+    if (n_vol <= 0 || !geoms || !ops || !field_a || !field_b || !codes || !flux_off || !csum_off || !d_mean ||
+        !desc_dev)
+        return TF_ERR_ARG;
+    return describe(n_vol, geoms, ops, field_a, field_b, codes, nullptr, flux_off, csum_off, d_mean, err_dev,
+                    desc_dev);
+}
+
+int tf_batch_describe_rhs(int n_vol, const tf_geom* geoms, const tf_operator* ops, float* const* field_a,
+                          float* const* field_b, const uint8_t* const* codes, const float* const* rhs,
+                          int32_t* err_dev, void* desc_dev) {
+    if (n_vol <= 0 || !geoms || !ops || !field_a || !field_b || !codes || !rhs || !desc_dev) return TF_ERR_ARG;
+    return describe(n_vol, geoms, ops, field_a, field_b, codes, rhs, nullptr, nullptr, nullptr, err_dev, desc_dev);
+}
+
+int tf_batch_advance_rhs(const void* desc_dev, const int32_t* work_dev, int n_work, const int32_t* launches_dev,
+                         int launch, void* stream) {
+    if (!desc_dev || !work_dev || n_work <= 0 || !launches_dev || launch < 0) return TF_ERR_ARG;
+    k_stream_multi_rhs<<<n_work, BShape::NT, BShape::SMEM, (cudaStream_t)stream>>>(
+        static_cast<const VolDesc*>(desc_dev), reinterpret_cast<const int2*>(work_dev), launches_dev, launch);
+    note_launch();
+    return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
 }
 
 int tf_batch_advance(const void* desc_dev, const int32_t* work_dev, int n_work, const int32_t* status_dev,

@@ -65,3 +65,18 @@ def test_batch_rejects_bad_input():
         tg.BatchSolve([np.full((8, 8, 8), 3)])
     with pytest.raises(tg.solvers._capi.TfError):
         tg.BatchSolve([random_binary((9, 9, 9), 1)], periodic=True)
+
+
+def test_batch_refine_with_dead_volume_and_repeat():
+    vols, periodic = _volumes()
+    dead = np.zeros((32, 32, 32), dtype=np.uint8)
+    dead[:20] = 1  # touches the inlet only: no spanning path
+    b = tg.BatchSolve(vols[:2] + [dead], periodic=periodic[:2] + [False])
+    res = b.solve(conv_crit=1e-3, refine={"tol": 1e-10})
+    assert np.all(res[2].D_eff == 0) and np.isinf(res[2].tau).all()
+    d1 = [r.D_eff.copy() for r in res[:2]]
+    assert all(r.residual_history[-1] < 1e-10 for r in res[:2])
+    res = b.refine(tol=1e-12)  # refining again starts from the refined field
+    for r, d in zip(res[:2], d1):
+        assert r.residual_history[0] < 1e-10 and r.residual_history[-1] < 1e-12
+        np.testing.assert_allclose(r.D_eff, d, rtol=1e-9)
