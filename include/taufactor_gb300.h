@@ -162,8 +162,10 @@ int tf_repack(const tf_geom* g, const tf_operator* op, const float* padded_dev, 
               void* stream);
 
 /* Self-check of the binary sweep's division: for divisor n in 1..8, count the float32 inputs s
- * (all finite bit patterns) where the kernel's exact division by n (one multiply and two FMAs
- * with RN(1/n)) differs bitwise from IEEE division s / n. Adds the count to *bad_dev (uint64).
+ * (all finite bit patterns) where the exact division by n (one multiply and two FMAs with
+ * RN(1/n)) differs bitwise from IEEE division s / n, where the sweeps' select-free form differs
+ * other than in the sign of a zero quotient, and where the SOR step c + w (q - c) with c = s
+ * differs between q = +0 and q = -0. Adds the count to *bad_dev (uint64).
  * No reference counterpart: it guards the bitwise parity of the update `sum / nn`
  * (taufactor.py:177). */
 int tf_check_small_division(int n, uint64_t* bad_dev, void* stream);

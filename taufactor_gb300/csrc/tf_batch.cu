@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(BShape::NT, 2)
     const int tz = item.y % d->tiles_z, ty = item.y / d->tiles_z;
     const SweepArgs a = parity ? d->ba : d->ab;
     stream_tile<TF_KIND_BINARY, BTY, BTZ, BK, false>(parity ? &d->map_b : &d->map_a, &d->map_c, a, nullptr,
-                                                     tz * (BTZ / 2), ty * BTY, 0, smem);
+                                                     tz * (BTZ / 2), ty * BTY, 0, 0, a.g.NX, smem);
 }
 
 // Correction sweeps: launch `launch` of an inner solve; volume v takes part while
@@ -64,7 +64,7 @@ __global__ void __launch_bounds__(BShape::NT, 2)
     const int parity = launch & 1;
     const SweepArgs a = parity ? d->ba : d->ab;
     stream_tile<TF_KIND_BINARY, BTY, BTZ, BK, true>(parity ? &d->map_b : &d->map_a, &d->map_c, a, nullptr,
-                                                    tz * (BTZ / 2), ty * BTY, 0, smem);
+                                                    tz * (BTZ / 2), ty * BTY, 0, 0, a.g.NX, smem);
 }
 
 // One CTA per (volume, plane): float64 sums of the masked x-flux through face x|x+1 and of the

@@ -130,7 +130,16 @@ __device__ __forceinline__ float div_small(float s, float n, float r) {
     return e == 0.0f ? q : __fmaf_rn(e, r, q);
 }
 
-// div_small with the tiny-dividend fallback used by the sweeps: exact for every finite s.
+// div_small without the zero test, as the binary sweeps use it: RN(q + e*r) also when e == 0.
+// It differs from IEEE division only for s = -0 (it returns +0 instead of -0), and the SOR step
+// c + omega * (quot - c) gives the same float32 bits for either zero quotient (quot - c is -c
+// for c != 0, and a zero c ends as +0 both ways), so the field stays bit-exact.
+__device__ __forceinline__ float div_small_fast(float s, float n, float r) {
+    const float q = __fmul_rn(s, r);
+    return __fmaf_rn(__fmaf_rn(-q, n, s), r, q);
+}
+
+// div_small with the tiny-dividend fallback: exact for every finite s.
 __device__ __forceinline__ float div_small_exact(float s, float n, float r) {
     return (s != 0.0f && fabsf(s) < 0x1p-90f) ? __fdiv_rn(s, n) : div_small(s, n, r);
 }

@@ -11,6 +11,9 @@ namespace tf {
 
 void note_launch();
 
+// Streaming multiprocessors of the current device (cached per device; 1 if unknown).
+int sm_count();
+
 // 3-D tiled tensor map over [dim2][dim1][dim0] with the given byte strides of dims 1 and 2.
 int encode_map_3d(CUtensorMap* map, const void* base, int elem_bytes, long long dim0, long long dim1,
                   long long dim2, long long stride1_bytes, long long stride2_bytes, int box0, int box1);

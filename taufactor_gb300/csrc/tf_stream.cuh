@@ -16,6 +16,11 @@
 // the tile interior is exact; it is written from registers to the other ping-pong buffer (plus
 // periodic ghost copies). The result is K reference iterations of taufactor.py:174-182,
 // bit for bit.
+//
+// A CTA may own only the planes [x0, x1) of its tile column (x-chunks, to even out the last
+// wave of CTAs): it streams planes [x0-K, x1+K) clipped to the volume. Below x0 the missing
+// x-1 neighbour corrupts one more plane per half-sweep, i.e. exactly the K margin planes; above
+// x1 the margin planes are only read, never needed at a later time. Planes [x0, x1) are exact.
 #pragma once
 
 #include "tf_common.cuh"
@@ -100,12 +105,14 @@ __device__ __forceinline__ void stage_update(float4& self, const float4& xp, con
 }
 
 // The CTA's work: one tile (j0 = first staged padded j, y0 = first interior row, volume b of
-// the batch described by `a`) for K half-sweeps. `op` may be null for the binary operator.
+// the batch described by `a`, written planes [x0, x1)) for K half-sweeps. `op` may be null for
+// the binary operator.
 // `tmf` / `tmc` are tensor maps of the input field and the codes (kernel parameter or global
 // memory). Shared memory: StreamShape::SMEM bytes at `smem` (128-byte aligned).
 template <int KIND, int TY, int TZ, int K, bool RHS>
 __device__ __forceinline__ void stream_tile(const CUtensorMap* tmf, const CUtensorMap* tmc, const SweepArgs& a,
-                                            const tf_operator* op, int j0, int y0, int b, unsigned char* smem) {
+                                            const tf_operator* op, int j0, int y0, int b, int x0, int x1,
+                                            unsigned char* smem) {
     using S = StreamShape<TY, TZ, K>;
     constexpr int G = S::G, WJ = S::WJ, WJC = S::WJC, NS = S::NS, D = S::D, R = S::R, NT = S::NT;
     constexpr int ROWS = S::ROWS;
@@ -147,18 +154,22 @@ __device__ __forceinline__ void stream_tile(const CUtensorMap* tmf, const CUtens
     }
     __syncthreads();
 
+    // streamed planes [xs, xe); plane x uses slot (x - xs) % NS, its ((x - xs) / NS)-th use
+    const int xs = x0 > K ? x0 - K : 0;
+    const int xe = x1 + K < NX ? x1 + K : NX;
     auto issue = [&](int x) {
-        const int s = x % NS;
+        const int s = (x - xs) % NS;
         mbar_arrive_expect_tx(&bar[s], S::FBYTES + S::CBYTES);
         tma_load_3d(F0 + s * (S::SLOT / 4), tmf, &bar[s], j0, row0, b * NX + x);
         tma_load_3d(C0 + s * S::SLOT, tmc, &bar[s], j0, row0, b * NX + x);
     };
     if (tid == 0)
-        for (int x = 0; x < D && x < NX; ++x) issue(x);
+        for (int x = xs; x < xs + D && x < xe; ++x) issue(x);
 
-    // own cells by relative colour (V0, V1) and their codes (K0, K1); ring index = plane % R.
+    // own cells by relative colour (V0, V1) and their codes (K0, K1); ring index = (plane - xs) % R.
     // Plane -1 (ring slot R-1 until plane R-1 arrives) and plane NX are the Dirichlet ghost
-    // planes 2*bc, so x-neighbours need no boundary selects.
+    // planes 2*bc, so x-neighbours need no boundary selects (a chunk starting above 0 reads the
+    // same constant as its plane xs-1: a margin plane).
     float4 V0[R], V1[R];
     uint32_t K0[R], K1[R];
 #pragma unroll
@@ -169,16 +180,17 @@ __device__ __forceinline__ void stream_tile(const CUtensorMap* tmf, const CUtens
 
     const bool interior_group = gi >= 1 && gi < G - 1;
     const bool py = a.periodic & TF_PERIODIC_Y, pz = a.periodic & TF_PERIODIC_Z;
-    const int total = NX + K;
-    for (int t0 = 0; t0 < total; t0 += R) {
+    // steps: the last chunk runs K past the volume (Dirichlet plane NX), the others stop at xe
+    const int total = xe == NX ? NX + K : xe;
+    for (int t0 = xs; t0 < total; t0 += R) {
 #pragma unroll
         for (int i = 0; i < R; ++i) {
             const int t = t0 + i;
             if (t < total) {
-                if (tid == 0 && t + D < NX) issue(t + D);
-                if (t < NX) {
-                    const int slot = t % NS;
-                    if (!mbar_wait_bounded(&bar[slot], (t / NS) & 1)) *s_fail = 1;
+                if (tid == 0 && t + D < xe) issue(t + D);
+                if (t < xe) {
+                    const int slot = (t - xs) % NS;
+                    if (!mbar_wait_bounded(&bar[slot], ((t - xs) / NS) & 1)) *s_fail = 1;
                     const float* Fs = F0 + slot * (S::SLOT / 4);
                     const unsigned char* Cs = C0 + slot * S::SLOT;
                     const float4 e4 = ld4(Fs + (2 * ty) * WJ + jj);
@@ -201,9 +213,9 @@ __device__ __forceinline__ void stream_tile(const CUtensorMap* tmf, const CUtens
                     const int ipp = (i - s - 1 + 2 * R) % R;
                     // rows [s, ROWS - s) form the region of half-sweep s: it shrinks by one row per
                     // half-sweep so the tile interior is exact after K of them
-                    if (p >= 0 && p < NX && ty >= s && ty < ROWS - s) {
-                        float* Fp = F0 + (p % NS) * (S::SLOT / 4);
-                        const unsigned char* Cp = C0 + (p % NS) * S::SLOT;
+                    if (p >= xs && p < NX && ty >= s && ty < ROWS - s) {
+                        float* Fp = F0 + ((p - xs) % NS) * (S::SLOT / 4);
+                        const unsigned char* Cp = C0 + ((p - xs) % NS) * S::SLOT;
                         const bool at_lo = p == 0, at_hi = p == NX - 1;
                         // relative colour (s-1)&1 updates; even-z cells hold relative colour (p+y+c0)&1
                         const int q = ((p + y + c0) & 1) ^ ((s - 1) & 1);  // half-row type being updated
@@ -231,7 +243,7 @@ __device__ __forceinline__ void stream_tile(const CUtensorMap* tmf, const CUtens
                 // write back plane t-K from registers
                 const int pw = t - K;
                 const int iw = (i - K + 2 * R) % R;
-                if (pw >= 0 && interior_group && ty >= K && ty < K + TY && y < g.NY) {
+                if (pw >= x0 && pw < x1 && interior_group && ty >= K && ty < K + TY && y < g.NY) {
                     const bool even0 = ((pw + y + c0) & 1) == 0;
                     const float4 ev = even0 ? V0[iw] : V1[iw];
                     const float4 od = even0 ? V1[iw] : V0[iw];
@@ -270,7 +282,8 @@ __device__ __forceinline__ void stream_tile(const CUtensorMap* tmf, const CUtens
                 __syncthreads();
                 if (*s_fail) {
                     if (tid == 0) {
-                        for (int x = t + 1; x < t + 1 + D && x < NX; ++x) mbar_wait_bounded(&bar[x % NS], (x / NS) & 1);
+                        for (int x = t + 1; x < t + 1 + D && x < xe; ++x)
+                            mbar_wait_bounded(&bar[(x - xs) % NS], ((x - xs) / NS) & 1);
                         if (a.err) atomicExch(a.err, TF_ERR_TIMEOUT);
                     }
                     return;
@@ -287,10 +300,30 @@ __global__ void __launch_bounds__(StreamShape<TY, TZ, K>::NT, StreamShape<TY, TZ
     // dynamic shared memory: the runtime aligns it to at least 128 bytes (no static shared
     // variables precede it in this kernel); every pointer below stays in the shared window
     extern __shared__ __align__(128) unsigned char smem[];
-    stream_tile<KIND, TY, TZ, K, RHS>(&tmf, &tmc, a, &op, blockIdx.x * (TZ / 2), blockIdx.y * TY, blockIdx.z, smem);
+    const int b = blockIdx.z / a.x_chunks, c = blockIdx.z - b * a.x_chunks;
+    const int x0 = (int)((long long)c * a.g.NX / a.x_chunks), x1 = (int)((long long)(c + 1) * a.g.NX / a.x_chunks);
+    stream_tile<KIND, TY, TZ, K, RHS>(&tmf, &tmc, a, &op, blockIdx.x * (TZ / 2), blockIdx.y * TY, b, x0, x1, smem);
 }
 
 // ------------------------------------------------------------------------------ host side
+// Number of x-chunks per tile column: minimises (waves of CTAs) x (steps per CTA), where a
+// chunk of nx/c planes costs nx/c + 2K steps and `slots` CTAs run at once. 1 when the
+// columns already fill the last wave well.
+inline int x_chunks_for(long long columns, int nx, int k, int slots) {
+    if (slots <= 0) return 1;
+    int best = 1;
+    double best_cost = 1e300;
+    for (int c = 1; c <= 8 && nx / c >= 8 * k; ++c) {
+        const long long waves = (columns * c + slots - 1) / slots;
+        const double cost = (double)waves * ((double)nx / c + (c > 1 ? 2 * k : k));
+        if (cost < best_cost * 0.995) {
+            best_cost = cost;
+            best = c;
+        }
+    }
+    return best;
+}
+
 template <int KIND, int TY, int TZ, int K, bool RHS>
 static int launch_stream(const tf_geom& gg, const tf_operator& op, const float* in, float* out, const uint8_t* code,
                          const float* rhs, int first_colour, int32_t* err, cudaStream_t st) {
@@ -303,15 +336,22 @@ static int launch_stream(const tf_geom& gg, const tf_operator& op, const float* 
                        (long long)gg.zhc * 2 * gg.yp, S::WJC, 2 * S::ROWS);
     if (rc) return rc;
     static bool attr_set = false;
+    static int resident = 1;  // CTAs of this kernel per SM
     auto kern = k_stream<KIND, TY, TZ, K, RHS>;
     if (!attr_set) {
         if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM) != cudaSuccess)
             return TF_ERR_CUDA;
+        int n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, S::NT, S::SMEM) == cudaSuccess && n > 0)
+            resident = n;
         attr_set = true;
     }
     SweepArgs a = make_args(make_geo(gg), op, out, first_colour, K, err);
     a.rhs = rhs;
-    dim3 grid((gg.nz + TZ - 1) / TZ, (gg.ny + TY - 1) / TY, gg.batch);
+    const long long columns = (long long)((gg.nz + TZ - 1) / TZ) * ((gg.ny + TY - 1) / TY) * gg.batch;
+    a.x_chunks = x_chunks_for(columns, gg.nx, K, resident * sm_count());
+    if ((long long)gg.batch * a.x_chunks > 65535) a.x_chunks = 1;  // grid z limit
+    dim3 grid((gg.nz + TZ - 1) / TZ, (gg.ny + TY - 1) / TY, gg.batch * a.x_chunks);
     kern<<<grid, S::NT, S::SMEM, st>>>(tmf, tmc, a, op);
     note_launch();
     return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;

@@ -112,6 +112,12 @@ __global__ void k_check_division(int n, unsigned long long* bad) {
         const float a = div_small_exact(s, nf, r);
         const float b = __fdiv_rn(s, nf);
         if (__float_as_uint(a) != __float_as_uint(b)) ++local;
+        // the sweeps' form: equal up to the sign of a zero quotient ...
+        const float f = (s != 0.0f && fabsf(s) < 0x1p-90f) ? __fdiv_rn(s, nf) : div_small_fast(s, nf, r);
+        if (__float_as_uint(f) != __float_as_uint(b) && !(f == 0.0f && b == 0.0f)) ++local;
+        // ... which the SOR step maps to the same bits (s taken as the old value c)
+        const float w = 1.0f + 0.125f * static_cast<float>(n);
+        if (__float_as_uint(sor_finish(s, 0.0f, w)) != __float_as_uint(sor_finish(s, -0.0f, w))) ++local;
     }
     if (local) atomicAdd(bad, local);
 }
@@ -129,6 +135,7 @@ SweepArgs make_args(const Geo& g, const tf_operator& op, float* out, int first_c
     a.g = g; a.out = out; a.omega = op.omega; a.glo = op.ghost_lo; a.ghi = op.ghost_hi;
     a.ky = op.ky; a.kz = op.kz; a.first_colour = first_colour & 1; a.n_half = n_half; a.err = err;
     a.periodic = op.periodic;
+    a.x_chunks = 1;
     a.rhs = nullptr;
     return a;
 }

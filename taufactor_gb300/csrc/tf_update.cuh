@@ -10,6 +10,7 @@ struct SweepArgs {
     float* out;
     float omega, glo, ghi, ky, kz;
     int first_colour, n_half, periodic;
+    int x_chunks;      // x-chunks per tile column of the fused sweep (grid z = batch * x_chunks)
     int32_t* err;
     const float* rhs;  // right-hand side of a correction solve (split layout), or null
 };
@@ -69,7 +70,7 @@ __device__ __forceinline__ float4 update4_binary(float4 c, const float4& xp, con
     const float2 t0 = tab[cc & 0xffu], t1 = tab[(cc >> 8) & 0xffu], t2 = tab[(cc >> 16) & 0xffu], t3 = tab[cc >> 24];
     n = make_float4(t0.x, t1.x, t2.x, t3.x);
     r = make_float4(t0.y, t1.y, t2.y, t3.y);
-#define TF_Q(L) q.L = div_small(s.L, n.L, r.L);
+#define TF_Q(L) q.L = div_small_fast(s.L, n.L, r.L);
     TF_LANES(TF_Q)
     // 0 < |sum| < 2^-90: the correction term can underflow, take IEEE division (never in practice;
     // a zero sum is exact on the fast path)

@@ -51,9 +51,11 @@ def test_half_sweeps_bitwise_vs_reference(name, golden):
 
 
 @pytest.mark.parametrize("kind", ["binary", "periodic", "anisotropic", "multiphase", "periodic_multiphase"])
-@pytest.mark.parametrize("shape", [(1, 23, 40, 70), (2, 9, 17, 33), (1, 5, 64, 128), (1, 30, 8, 16)])
+@pytest.mark.parametrize("shape", [(1, 23, 40, 70), (2, 9, 17, 33), (1, 5, 64, 128), (1, 30, 8, 16),
+                                   (1, 100, 24, 40)])
 def test_chunked_half_sweeps_bitwise_vs_oracle(kind, shape):
-    """Every chunk length 1..9 (several tiled launches, odd/even colour starts) matches."""
+    """Every chunk length 1..9 (several tiled launches, odd/even colour starts) matches. The
+    long-x shape runs each tile column as several x-chunks (few columns for 152 SMs)."""
     seed = sum(shape)
     if kind in ("multiphase", "periodic_multiphase"):
         img = random_labels(shape, seed)
@@ -181,9 +183,11 @@ def test_small_integer_division_is_ieee():
 @pytest.mark.parametrize("k_max", [2, 3, 4])
 @pytest.mark.parametrize("tile", [0, 1, 2])
 @pytest.mark.parametrize("kind", ["binary", "periodic"])
-def test_tile_variants_bitwise(kind, tile, k_max):
-    """Every tile shape and fused depth of the kernel gives the reference iterations bit for bit."""
-    img = random_binary((2, 21, 52, 136), 31 + tile)
+@pytest.mark.parametrize("shape", [(2, 21, 52, 136), (1, 150, 20, 40)])
+def test_tile_variants_bitwise(kind, tile, k_max, shape):
+    """Every tile shape and fused depth of the kernel gives the reference iterations bit for bit;
+    the second shape splits every tile column into 4-8 x-chunks of uneven length."""
+    img = random_binary(shape, 31 + tile)
     o = OracleSolve(img, kind=kind)
     s = make_solver(kind, img, {})
     s._op.tile = tile
