@@ -34,7 +34,9 @@ def sources():
 
 def _compile(nvcc, src, verbose_ptxas=False):
     obj = os.path.join(OBJ, os.path.basename(src)[:-3] + ".o")
-    cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-c", src, "-o", obj]
+    # -fmad=false: no multiply-add contraction anywhere; every fused operation in the kernels is
+    # an explicit fma (the float32 sweeps must round every product and sum on its own).
+    cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-fmad=false", "-Xcompiler", "-fPIC", "-c", src, "-o", obj]
     if verbose_ptxas:
         cmd += ["-Xptxas", "-v"]
     r = subprocess.run(cmd, capture_output=True, text=True)

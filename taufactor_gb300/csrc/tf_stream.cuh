@@ -45,8 +45,9 @@ struct StreamShape {
     static constexpr int GUARD = 128;                // readable guard around each field slot
     static constexpr int FSPAN = (GUARD + FBYTES + GUARD + 127) / 128 * 128;
     static constexpr int SLOT = FSPAN + (CBYTES + 127) / 128 * 128;
-    static constexpr int LUT_BYTES = 32 * 32 * 4;
-    static constexpr int HEAD = 128 + LUT_BYTES + 128;  // mbarriers, LUT, division table
+    // operator table: multiphase faces (4 KB), anisotropic divisors or the binary division table
+    static constexpr int LUT_BYTES = (DIV_TABLE_BYTES > 32 * 32 * 4 ? DIV_TABLE_BYTES : 32 * 32 * 4) / 128 * 128 + 128;
+    static constexpr int HEAD = 128 + LUT_BYTES + 128;  // mbarriers, LUT (binary: division table)
     static constexpr int SMEM = HEAD + NS * SLOT;
     static_assert(TJ % 16 == 0, "tile z-extent must keep TMA box starts 16-byte aligned for codes");
     static_assert(K >= 1 && K <= HY, "half-sweeps per launch exceed the ghost rows");
@@ -81,7 +82,7 @@ __device__ __forceinline__ void stage_update(float4& self, const float4& xp, con
                                              uint32_t cc, uint32_t cxp, uint32_t cxm, uint32_t czo, float* Fp,
                                              const unsigned char* Cp, int row_up, int row_dn, int row_me, int row_ot,
                                              int jj, int q, int WJ, int WJC, bool at_lo, bool at_hi,
-                                             const SweepArgs& a, const float* lut, const float2* tab,
+                                             const SweepArgs& a, const float* lut, const float4* tab,
                                              const float* rhs_row) {
     // right-hand side of a correction solve (A e = r): the thread's 4 cells, read-only path
     float4 rv = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -119,7 +120,9 @@ __device__ __forceinline__ void stream_tile(const CUtensorMap* tmf, const CUtens
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
     int* s_fail = reinterpret_cast<int*>(smem + 8 * NS);
     float* lut = reinterpret_cast<float*>(smem + 128);
-    float2* tab = reinterpret_cast<float2*>(smem + 128 + S::LUT_BYTES);
+    // binary: the pair division table in the LUT area (the LUT serves the other operators)
+    float4* tab_all = reinterpret_cast<float4*>(smem + 128);
+    const float4* tab = division_copy(tab_all);
     float* const F0 = reinterpret_cast<float*>(smem + S::HEAD + S::GUARD);
     unsigned char* const C0 = smem + S::HEAD + S::FSPAN;
 
@@ -144,7 +147,7 @@ __device__ __forceinline__ void stream_tile(const CUtensorMap* tmf, const CUtens
         for (int i = tid; i < 256; i += NT) lut[i] = op->divisor[i];
     if (KIND == TF_KIND_MULTIPHASE)
         for (int i = tid; i < 32 * 32; i += NT) lut[i] = op->face[i];
-    fill_division_table(tab, tid);
+    if (KIND == TF_KIND_BINARY) fill_division_table(tab_all, tid, NT);
     for (int s = 0; s < NS; ++s) {
         float* f = F0 + s * (S::SLOT / 4);
         for (int i = tid; i < S::GUARD / 4; i += NT) {
@@ -369,17 +372,27 @@ static int dispatch_k(const tf_geom& g, const tf_operator& op, const float* in, 
     return TF_ERR_ARG;
 }
 
-// Tile shapes (op.tile): 0 = 16x64, 1 = 16x128, 2 = 32x64 (rows x z-cells). The multiphase and
-// anisotropic operators, and every correction solve with a right-hand side, use shape 0.
+// Tile shapes (op.tile) of the binary operator: 0 = 16x64, 1 = 16x128, 2 = 32x64 (rows x
+// z-cells); shapes 1 and 2 fuse 2..4 half-sweeps (a single half-sweep runs on shape 0). The
+// multiphase and anisotropic operators, and every correction solve with a right-hand side, use
+// shape 0. Each shape's instantiations live in their own translation unit.
 template <int KIND>
 static int dispatch_kind(const tf_geom& g, const tf_operator& op, const float* in, float* out, const uint8_t* code,
                          const float* rhs, int first_colour, int n_half, int32_t* err, cudaStream_t st) {
     if (rhs) return dispatch_k<KIND, 16, 64, true>(g, op, in, out, code, rhs, first_colour, n_half, err, st);
-    if (KIND == TF_KIND_BINARY && op.tile == 1)
-        return dispatch_k<KIND, 16, 128, false>(g, op, in, out, code, nullptr, first_colour, n_half, err, st);
-    if (KIND == TF_KIND_BINARY && op.tile == 2)
-        return dispatch_k<KIND, 32, 64, false>(g, op, in, out, code, nullptr, first_colour, n_half, err, st);
     return dispatch_k<KIND, 16, 64, false>(g, op, in, out, code, nullptr, first_colour, n_half, err, st);
+}
+
+// K = 2..4 on one tile shape (shapes 1 and 2 of the binary operator).
+template <int TY, int TZ>
+static int dispatch_k234(const tf_geom& g, const tf_operator& op, const float* in, float* out, const uint8_t* code,
+                         int first_colour, int n_half, int32_t* err, cudaStream_t st) {
+    switch (n_half) {
+        case 2: return launch_stream<TF_KIND_BINARY, TY, TZ, 2, false>(g, op, in, out, code, nullptr, first_colour, err, st);
+        case 3: return launch_stream<TF_KIND_BINARY, TY, TZ, 3, false>(g, op, in, out, code, nullptr, first_colour, err, st);
+        case 4: return launch_stream<TF_KIND_BINARY, TY, TZ, 4, false>(g, op, in, out, code, nullptr, first_colour, err, st);
+    }
+    return TF_ERR_ARG;
 }
 
 }  // namespace tf

@@ -23,12 +23,12 @@ template <int KIND, bool RHS>
 __global__ void __launch_bounds__(256) k_plain(float* __restrict__ f, const uint8_t* __restrict__ code,
                                                const SweepArgs a, const __grid_constant__ tf_operator op, int colour) {
     __shared__ float lut[32 * 32];
-    __shared__ float2 tab[16];
+    __shared__ float4 tab[DIV_PAIRS * DIV_COPIES];
     if (KIND == TF_KIND_ANISOTROPIC)
         for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = op.divisor[i];
     if (KIND == TF_KIND_MULTIPHASE)
         for (int i = threadIdx.x; i < 32 * 32; i += blockDim.x) lut[i] = op.face[i];
-    fill_division_table(tab, threadIdx.x);
+    if (KIND == TF_KIND_BINARY) fill_division_table(tab, threadIdx.x, blockDim.x);
     __syncthreads();
     const Geo& g = a.g;
     const int gmax = (half_len(g.NZ, 0) + 3) >> 2;
@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(256) k_plain(float* __restrict__ f, const uint
     float4 rv = make_float4(0.f, 0.f, 0.f, 0.f);
     if (RHS) rv = *reinterpret_cast<const float4*>(a.rhs + base + q * g.ZH + HJ + j);
     const float4 nv = update4<KIND, RHS>(c, xp, xm, yp, ym, zp, zm, cc, cxp, cxm, cyp, cym, czp, czm, x == 0,
-                                         x == g.NX - 1, a.omega, a.ky, a.kz, lut, tab, rv);
+                                         x == g.NX - 1, a.omega, a.ky, a.kz, lut, division_copy(tab), rv);
     float* dst = f + base + q * g.ZH + HJ + j;
     for (int i = 0; i < 4 && j + i < nj; ++i) dst[i] = comp(nv, i);
 }

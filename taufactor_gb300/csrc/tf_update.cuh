@@ -28,11 +28,57 @@ __device__ __forceinline__ void set_comp(float4& v, int i, float f) {
 __device__ __forceinline__ uint32_t byte_of(uint32_t w, int i) { return (w >> (8 * i)) & 0xffu; }
 __device__ __forceinline__ uint32_t ld_u32(const unsigned char* p) { return *reinterpret_cast<const uint32_t*>(p); }
 
-// Binary division table: entry n = (n, RN(1/n)) for n = 1..8, entry 0 = (1, 0).
-__device__ __forceinline__ void fill_division_table(float2* tab, int tid) {
-    if (tid < 16) tab[tid] = tid == 0 ? make_float2(1.0f, 0.0f)
-                           : make_float2(static_cast<float>(tid), __frcp_rn(static_cast<float>(tid)));
+// Two float32 values in one 64-bit register pair, for the packed f32x2 instructions of
+// sm_100+ (each lane rounds exactly like the scalar instruction). Never feed mul2 into add2 or
+// sub2 where the product's own rounding matters: the assembler may fuse that pair.
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 pk2(float lo, float hi) {
+    f32x2 r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
 }
+__device__ __forceinline__ void upk2(f32x2 v, float& lo, float& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
+    f32x2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+    f32x2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+// Binary division table for two cells at once: pair e = lo * 9 + hi of neighbour counts lo, hi
+// in 0..8 holds (-n_lo, -n_hi, RN(1/n_lo), RN(1/n_hi)) with n = count, except count 0 -> n = 1,
+// 1/n = 0 (a frozen voxel: the reference's division by inf). Each pair is stored 8 times
+// (float4 at e * 8 + lane % 8), so the 8 threads of one phase of a 128-bit shared load always
+// hit different banks. 81 * 8 float4 = 10368 bytes. Counts are masked to 4 bits before the
+// lookup, which keeps any index inside the CTA's shared memory.
+constexpr int DIV_PAIRS = 81;
+constexpr int DIV_COPIES = 8;
+constexpr int DIV_TABLE_BYTES = DIV_PAIRS * DIV_COPIES * 16;
+__device__ __forceinline__ void fill_division_table(float4* tab, int tid, int nthreads) {
+    for (int i = tid; i < DIV_PAIRS * DIV_COPIES; i += nthreads) {
+        const int e = i / DIV_COPIES, lo = e / 9, hi = e - 9 * (e / 9);
+        const float nl = lo ? static_cast<float>(lo) : 1.0f, nh = hi ? static_cast<float>(hi) : 1.0f;
+        tab[i] = make_float4(-nl, -nh, lo ? __frcp_rn(nl) : 0.0f, hi ? __frcp_rn(nh) : 0.0f);
+    }
+}
+// This thread's copy of the table (copy lane % 8).
+__device__ __forceinline__ const float4* division_copy(const float4* tab) { return tab + (threadIdx.x & 7); }
 
 // Quotients sum / n by IEEE division, for the (rare) group in which some |sum| < 2^-90; kept
 // out of line so the sweeps' hot code stays small.
@@ -47,50 +93,60 @@ static __device__ __noinline__ float4 tiny_quotients(float4 sum, float4 n, float
 
 #define TF_LANES(OP) OP(x) OP(y) OP(z) OP(w)
 
-// Binary / periodic update of a float4 group, written lane-interleaved so the four dependency
-// chains overlap: sum in the order of taufactor.py:97-102 (x+1, x-1, y+1, y-1, z+1, z-1),
-// exact division by the neighbour count (table entry (n, RN(1/n)); code 0 -> (1, 0) gives the
-// reference's sum/inf = signed zero), then inc = q - c; inc *= omega; c += inc (:177-181).
+// Binary / periodic update of a float4 group as two packed lane pairs (x, y) and (z, w): sum
+// in the order of taufactor.py:97-102 (x+1, x-1, y+1, y-1, z+1, z-1), exact division by the
+// neighbour count (div_small_fast with the pair table; count 0 gives the reference's
+// sum/inf = signed zero), then inc = q - c; inc *= omega; c += inc (:177-181). Every packed
+// instruction rounds each lane like its scalar counterpart, so the result is the scalar one.
+// `tab` is this thread's copy of the division table (division_copy).
 template <bool RHS>
 __device__ __forceinline__ float4 update4_binary(float4 c, const float4& xp, const float4& xm, const float4& yp,
                                                  const float4& ym, const float4& zp, const float4& zm, uint32_t cc,
-                                                 float omega, const float2* tab, const float4& rv) {
-    float4 s, n, r, q;
-#define TF_S1(L) s.L = __fadd_rn(xp.L, xm.L);
-#define TF_S2(L) s.L = __fadd_rn(s.L, yp.L);
-#define TF_S3(L) s.L = __fadd_rn(s.L, ym.L);
-#define TF_S4(L) s.L = __fadd_rn(s.L, zp.L);
-#define TF_S5(L) s.L = __fadd_rn(s.L, zm.L);
-    TF_LANES(TF_S1) TF_LANES(TF_S2) TF_LANES(TF_S3) TF_LANES(TF_S4) TF_LANES(TF_S5)
+                                                 float omega, const float4* tab, const float4& rv) {
+    f32x2 s0 = add2(pk2(xp.x, xp.y), pk2(xm.x, xm.y));
+    f32x2 s1 = add2(pk2(xp.z, xp.w), pk2(xm.z, xm.w));
+    s0 = add2(s0, pk2(yp.x, yp.y));
+    s1 = add2(s1, pk2(yp.z, yp.w));
+    s0 = add2(s0, pk2(ym.x, ym.y));
+    s1 = add2(s1, pk2(ym.z, ym.w));
+    s0 = add2(s0, pk2(zp.x, zp.y));
+    s1 = add2(s1, pk2(zp.z, zp.w));
+    s0 = add2(s0, pk2(zm.x, zm.y));
+    s1 = add2(s1, pk2(zm.z, zm.w));
     if (RHS) {
-#define TF_S6(L) s.L = __fadd_rn(s.L, rv.L);
-        TF_LANES(TF_S6)
-#undef TF_S6
+        s0 = add2(s0, pk2(rv.x, rv.y));
+        s1 = add2(s1, pk2(rv.z, rv.w));
     }
-    const float2 t0 = tab[cc & 0xffu], t1 = tab[(cc >> 8) & 0xffu], t2 = tab[(cc >> 16) & 0xffu], t3 = tab[cc >> 24];
-    n = make_float4(t0.x, t1.x, t2.x, t3.x);
-    r = make_float4(t0.y, t1.y, t2.y, t3.y);
-#define TF_Q(L) q.L = div_small_fast(s.L, n.L, r.L);
-    TF_LANES(TF_Q)
+    const float4 t0 = tab[((cc & 0xfu) * 9u + ((cc >> 8) & 0xfu)) * DIV_COPIES];
+    const float4 t1 = tab[(((cc >> 16) & 0xfu) * 9u + ((cc >> 24) & 0xfu)) * DIV_COPIES];
+    const f32x2 r0 = pk2(t0.z, t0.w), r1 = pk2(t1.z, t1.w);
+    f32x2 q0 = mul2(s0, r0), q1 = mul2(s1, r1);
+    q0 = fma2(fma2(q0, pk2(t0.x, t0.y), s0), r0, q0);
+    q1 = fma2(fma2(q1, pk2(t1.x, t1.y), s1), r1, q1);
     // 0 < |sum| < 2^-90: the correction term can underflow, take IEEE division (never in practice;
     // a zero sum is exact on the fast path)
+    float4 s;
+    upk2(s0, s.x, s.y);
+    upk2(s1, s.z, s.w);
     const float tiny = 0x1p-90f;
-    const float m = fminf(fminf(fabsf(s.x) == 0.0f ? 1.0f : fabsf(s.x), fabsf(s.y) == 0.0f ? 1.0f : fabsf(s.y)),
-                          fminf(fabsf(s.z) == 0.0f ? 1.0f : fabsf(s.z), fabsf(s.w) == 0.0f ? 1.0f : fabsf(s.w)));
-    if (m < tiny) q = tiny_quotients(s, n, r);
-#define TF_F1(L) q.L = __fsub_rn(q.L, c.L);
-#define TF_F2(L) q.L = __fmul_rn(q.L, omega);
-#define TF_F3(L) c.L = __fadd_rn(c.L, q.L);
-    TF_LANES(TF_F1) TF_LANES(TF_F2) TF_LANES(TF_F3)
-#undef TF_S1
-#undef TF_S2
-#undef TF_S3
-#undef TF_S4
-#undef TF_S5
-#undef TF_Q
-#undef TF_F1
-#undef TF_F2
-#undef TF_F3
+    const bool any_tiny = (fabsf(s.x) < tiny && s.x != 0.0f) || (fabsf(s.y) < tiny && s.y != 0.0f) ||
+                          (fabsf(s.z) < tiny && s.z != 0.0f) || (fabsf(s.w) < tiny && s.w != 0.0f);
+    if (any_tiny) {
+        const float4 q = tiny_quotients(s, make_float4(-t0.x, -t0.y, -t1.x, -t1.y), make_float4(t0.z, t0.w, t1.z, t1.w));
+        q0 = pk2(q.x, q.y);
+        q1 = pk2(q.z, q.w);
+    }
+    // inc * omega with scalar mul.rn: a packed multiply feeding the packed add below can be
+    // merged into one fused operation by the assembler (its .rn does not prevent that), which
+    // would skip the rounding of the product; scalar mul.rn is never contracted
+    const f32x2 c0 = pk2(c.x, c.y), c1 = pk2(c.z, c.w);
+    float i0, i1, i2, i3;
+    upk2(sub2(q0, c0), i0, i1);
+    upk2(sub2(q1, c1), i2, i3);
+    q0 = add2(c0, pk2(__fmul_rn(i0, omega), __fmul_rn(i1, omega)));
+    q1 = add2(c1, pk2(__fmul_rn(i2, omega), __fmul_rn(i3, omega)));
+    upk2(q0, c.x, c.y);
+    upk2(q1, c.z, c.w);
     return c;
 }
 
@@ -106,25 +162,14 @@ __device__ __forceinline__ float4 update4(float4 c, const float4& xp, const floa
                                           const float4& ym, const float4& zp, const float4& zm, uint32_t cc,
                                           uint32_t cxp, uint32_t cxm, uint32_t cyp, uint32_t cym, uint32_t czp,
                                           uint32_t czm, bool at_lo, bool at_hi, float omega, float ky, float kz,
-                                          const float* lut, const float2* tab,
+                                          const float* lut, const float4* tab,
                                           const float4& rv = make_float4(0.f, 0.f, 0.f, 0.f)) {
     if (KIND == TF_KIND_BINARY) return update4_binary<RHS>(c, xp, xm, yp, ym, zp, zm, cc, omega, tab, rv);
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
         const float ci = comp(c, i);
         float sum, quot;
-        if (KIND == TF_KIND_BINARY) {
-            // sum order of taufactor.py:97-102: x+1, x-1, y+1, y-1, z+1, z-1
-            sum = __fadd_rn(comp(xp, i), comp(xm, i));
-            sum = __fadd_rn(sum, comp(yp, i));
-            sum = __fadd_rn(sum, comp(ym, i));
-            sum = __fadd_rn(sum, comp(zp, i));
-            sum = __fadd_rn(sum, comp(zm, i));
-            const float2 nr = tab[byte_of(cc, i)];
-            quot = div_small(sum, nr.x, nr.y);
-            // below 2^-90 the correction term can underflow; take IEEE division there
-            if (fabsf(sum) < 0x1p-90f) quot = nr.y == 0.0f ? __fmul_rn(sum, 0.0f) : __fdiv_rn(sum, nr.x);
-        } else if (KIND == TF_KIND_ANISOTROPIC) {
+        if (KIND == TF_KIND_ANISOTROPIC) {
             // taufactor.py:475-477: (x+1 + x-1) + Ky*(y+1 + y-1) + Kz*(z+1 + z-1)
             sum = __fadd_rn(comp(xp, i), comp(xm, i));
             sum = __fadd_rn(sum, __fmul_rn(ky, __fadd_rn(comp(yp, i), comp(ym, i))));
