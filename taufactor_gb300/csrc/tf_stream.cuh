@@ -182,6 +182,10 @@ __device__ __forceinline__ void stream_tile(const CUtensorMap* tmf, const CUtens
     }
 
     const bool interior_group = gi >= 1 && gi < G - 1;
+    // bit s: this row lies in the region [s, ROWS - s) of half-sweep s
+    uint32_t stage_rows = 0;
+#pragma unroll
+    for (int s = 1; s <= K; ++s) stage_rows |= (ty >= s && ty < ROWS - s) ? (1u << s) : 0u;
     const bool py = a.periodic & TF_PERIODIC_Y, pz = a.periodic & TF_PERIODIC_Z;
     // steps: the last chunk runs K past the volume (Dirichlet plane NX), the others stop at xe
     const int total = xe == NX ? NX + K : xe;
@@ -216,7 +220,7 @@ __device__ __forceinline__ void stream_tile(const CUtensorMap* tmf, const CUtens
                     const int ipp = (i - s - 1 + 2 * R) % R;
                     // rows [s, ROWS - s) form the region of half-sweep s: it shrinks by one row per
                     // half-sweep so the tile interior is exact after K of them
-                    if (p >= xs && p < NX && ty >= s && ty < ROWS - s) {
+                    if (p >= xs && p < NX && (stage_rows & (1u << s))) {
                         float* Fp = F0 + ((p - xs) % NS) * (S::SLOT / 4);
                         const unsigned char* Cp = C0 + ((p - xs) % NS) * S::SLOT;
                         const bool at_lo = p == 0, at_hi = p == NX - 1;

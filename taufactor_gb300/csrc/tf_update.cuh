@@ -117,21 +117,23 @@ __device__ __forceinline__ float4 update4_binary(float4 c, const float4& xp, con
         s0 = add2(s0, pk2(rv.x, rv.y));
         s1 = add2(s1, pk2(rv.z, rv.w));
     }
-    const float4 t0 = tab[((cc & 0xfu) * 9u + ((cc >> 8) & 0xfu)) * DIV_COPIES];
-    const float4 t1 = tab[(((cc >> 16) & 0xfu) * 9u + ((cc >> 24) & 0xfu)) * DIV_COPIES];
+    // pair index 9 lo + hi of the 4-bit-masked counts, one byte dot product per pair
+    const int cm = static_cast<int>(cc & 0x0f0f0f0fu);
+    const float4 t0 = tab[__dp4a(cm, 0x00000109, 0) * DIV_COPIES];
+    const float4 t1 = tab[__dp4a(cm, 0x01090000, 0) * DIV_COPIES];
     const f32x2 r0 = pk2(t0.z, t0.w), r1 = pk2(t1.z, t1.w);
     f32x2 q0 = mul2(s0, r0), q1 = mul2(s1, r1);
     q0 = fma2(fma2(q0, pk2(t0.x, t0.y), s0), r0, q0);
     q1 = fma2(fma2(q1, pk2(t1.x, t1.y), s1), r1, q1);
-    // 0 < |sum| < 2^-90: the correction term can underflow, take IEEE division (never in practice;
-    // a zero sum is exact on the fast path)
+    // 0 < |sum| <= 2^-90: the correction term can underflow, take IEEE division (never in
+    // practice; a zero sum is exact on the fast path). Each lane's bit pattern minus one is
+    // |sum| less one ulp in magnitude, or a NaN for +-0, which fminf skips.
     float4 s;
     upk2(s0, s.x, s.y);
     upk2(s1, s.z, s.w);
-    const float tiny = 0x1p-90f;
-    const bool any_tiny = (fabsf(s.x) < tiny && s.x != 0.0f) || (fabsf(s.y) < tiny && s.y != 0.0f) ||
-                          (fabsf(s.z) < tiny && s.z != 0.0f) || (fabsf(s.w) < tiny && s.w != 0.0f);
-    if (any_tiny) {
+    const float m = fminf(fminf(fabsf(__int_as_float(__float_as_int(s.x) - 1)), fabsf(__int_as_float(__float_as_int(s.y) - 1))),
+                          fminf(fabsf(__int_as_float(__float_as_int(s.z) - 1)), fabsf(__int_as_float(__float_as_int(s.w) - 1))));
+    if (m < 0x1p-90f) {
         const float4 q = tiny_quotients(s, make_float4(-t0.x, -t0.y, -t1.x, -t1.y), make_float4(t0.z, t0.w, t1.z, t1.w));
         q0 = pk2(q.x, q.y);
         q1 = pk2(q.z, q.w);
