@@ -72,37 +72,50 @@ static __device__ __noinline__ void ghost_copies_scalar(float* outp, long long r
     }
 }
 
+// Offsets (elements) of one thread's cells within a plane's shared-memory slot for the half-row
+// q updated in a step: its own group (`me`; the y-neighbours are me -+ 2 WJ) and the z-edge cell
+// of the adjacent group in the other half-row (`e`). The same for every half-sweep of the step.
+struct SlotOffsets {
+    int me, e;
+};
+__device__ __forceinline__ SlotOffsets slot_offsets(int ty, int jj, int q, int W) {
+    SlotOffsets o;
+    o.me = (2 * ty + q) * W + jj;
+    o.e = (2 * ty + (q ^ 1)) * W + (q ? jj + 4 : jj - 1);
+    return o;
+}
+
 // One half-sweep on the thread's float4 group at plane p (relative colour held in `self`).
 //   xp/xm: x-neighbour groups (registers; Dirichlet ghost planes are part of the ring);
 //   zo: the other half-row group of this plane (registers); y-neighbours and the z-edge cell of
-//   the adjacent group are read from the plane's shared-memory slot, and the result is
-//   published there.
+//   the adjacent group are read from the plane's shared-memory slot (field offsets fo, code
+//   offsets co), and the result is published there.
 template <int KIND, bool RHS>
 __device__ __forceinline__ void stage_update(float4& self, const float4& xp, const float4& xm, const float4& zo,
                                              uint32_t cc, uint32_t cxp, uint32_t cxm, uint32_t czo, float* Fp,
-                                             const unsigned char* Cp, int row_up, int row_dn, int row_me, int row_ot,
-                                             int jj, int q, int WJ, int WJC, bool at_lo, bool at_hi,
-                                             const SweepArgs& a, const float* lut, const float4* tab,
-                                             const float* rhs_row) {
+                                             const unsigned char* Cp, SlotOffsets fo, SlotOffsets co, int q, int WJ,
+                                             int WJC, bool at_lo, bool at_hi, const SweepArgs& a, const float* lut,
+                                             const float4* tab, const float* rhs_row) {
     // right-hand side of a correction solve (A e = r): the thread's 4 cells, read-only path
     float4 rv = make_float4(0.f, 0.f, 0.f, 0.f);
     if (RHS && rhs_row) rv = __ldg(reinterpret_cast<const float4*>(rhs_row + q * a.g.ZH));
-    const float4 yp = ld4(Fp + row_up * WJ + jj);
-    const float4 ym = ld4(Fp + row_dn * WJ + jj);
-    const int ej = q ? jj + 4 : jj - 1;
-    const float e = Fp[row_ot * WJ + ej];
+    const float4 yp = ld4(Fp + fo.me + 2 * WJ);
+    const float4 ym = ld4(Fp + fo.me - 2 * WJ);
+    const float e = Fp[fo.e];
     float4 zp, zm;
     z_neighbours(q, zo, e, zp, zm);
     uint32_t cyp = 0, cym = 0, czp = 0, czm = 0;
     if (KIND == TF_KIND_MULTIPHASE) {
-        cyp = ld_u32(Cp + row_up * WJC + jj);
-        cym = ld_u32(Cp + row_dn * WJC + jj);
-        const uint32_t ce = (ej >= 0 && ej < WJC) ? Cp[row_ot * WJC + ej] : 0u;
+        cyp = ld_u32(Cp + co.me + 2 * WJC);
+        cym = ld_u32(Cp + co.me - 2 * WJC);
+        // z-edge code: inside the slot for every thread (a halo group may read the edge code of
+        // the neighbouring staged row, which only affects halo cells)
+        const uint32_t ce = Cp[co.e];
         z_codes(q, czo, ce, czp, czm);
     }
     self = update4<KIND, RHS>(self, xp, xm, yp, ym, zp, zm, cc, cxp, cxm, cyp, cym, czp, czm, at_lo, at_hi, a.omega,
                               a.ky, a.kz, lut, tab, rv);
-    st4(Fp + row_me * WJ + jj, self);
+    st4(Fp + fo.me, self);
 }
 
 // The CTA's work: one tile (j0 = first staged padded j, y0 = first interior row, volume b of
@@ -187,6 +200,7 @@ __device__ __forceinline__ void stream_tile(const CUtensorMap* tmf, const CUtens
 #pragma unroll
     for (int s = 1; s <= K; ++s) stage_rows |= (ty >= s && ty < ROWS - s) ? (1u << s) : 0u;
     const bool py = a.periodic & TF_PERIODIC_Y, pz = a.periodic & TF_PERIODIC_Z;
+
     // steps: the last chunk runs K past the volume (Dirichlet plane NX), the others stop at xe
     const int total = xe == NX ? NX + K : xe;
     for (int t0 = xs; t0 < total; t0 += R) {
@@ -212,6 +226,11 @@ __device__ __forceinline__ void stream_tile(const CUtensorMap* tmf, const CUtens
                 } else if (t == NX) {
                     V0[i] = V1[i] = ghi4;
                 }
+                // every half-sweep of step t updates half-row (t + y + c0 + 1) & 1 of its plane: the
+                // relative colour (s-1)&1 sits in half-row (p + y + c0) & 1 ^ (s-1)&1, p = t - s
+                const int qs = (t + y + c0 + 1) & 1;
+                const SlotOffsets fo = slot_offsets(ty, jj, qs, WJ);
+                const SlotOffsets co = slot_offsets(ty, jj, qs, WJC);
 #pragma unroll
                 for (int s = 1; s <= K; ++s) {
                     const int p = t - s;
@@ -224,10 +243,6 @@ __device__ __forceinline__ void stream_tile(const CUtensorMap* tmf, const CUtens
                         float* Fp = F0 + ((p - xs) % NS) * (S::SLOT / 4);
                         const unsigned char* Cp = C0 + ((p - xs) % NS) * S::SLOT;
                         const bool at_lo = p == 0, at_hi = p == NX - 1;
-                        // relative colour (s-1)&1 updates; even-z cells hold relative colour (p+y+c0)&1
-                        const int q = ((p + y + c0) & 1) ^ ((s - 1) & 1);  // half-row type being updated
-                        const int row_up = 2 * (ty + 1) + q, row_dn = 2 * (ty - 1) + q, row_me = 2 * ty + q;
-                        const int row_ot = 2 * ty + (q ^ 1);
                         // global address of this thread's group in the right-hand side (padded
                         // coordinates; rows beyond the ghost bands and groups past the row read 0)
                         const float* rhs_row = nullptr;
@@ -237,13 +252,11 @@ __device__ __forceinline__ void stream_tile(const CUtensorMap* tmf, const CUtens
                         if (((s - 1) & 1) == 0) {
                             const uint32_t cxp = at_hi ? K0[ip] : K1[ipn], cxm = at_lo ? K0[ip] : K1[ipp];
                             stage_update<KIND, RHS>(V0[ip], V1[ipn], V1[ipp], V1[ip], K0[ip], cxp, cxm, K1[ip], Fp,
-                                                    Cp, row_up, row_dn, row_me, row_ot, jj, q, WJ, WJC, at_lo, at_hi,
-                                                    a, lut, tab, rhs_row);
+                                                    Cp, fo, co, qs, WJ, WJC, at_lo, at_hi, a, lut, tab, rhs_row);
                         } else {
                             const uint32_t cxp = at_hi ? K1[ip] : K0[ipn], cxm = at_lo ? K1[ip] : K0[ipp];
                             stage_update<KIND, RHS>(V1[ip], V0[ipn], V0[ipp], V0[ip], K1[ip], cxp, cxm, K0[ip], Fp,
-                                                    Cp, row_up, row_dn, row_me, row_ot, jj, q, WJ, WJC, at_lo, at_hi,
-                                                    a, lut, tab, rhs_row);
+                                                    Cp, fo, co, qs, WJ, WJC, at_lo, at_hi, a, lut, tab, rhs_row);
                         }
                     }
                 }
