@@ -196,7 +196,12 @@ def run_ours(args):
         torch.cuda.synchronize()
 
     s = tg.Solver(vols, device=dev)
-    tuning = {f"tile{t}_k{k}": round(ms, 5) for (t, k), ms in s.tune().items()}
+    if args.tile is not None:  # fixed kernel configuration (e.g. to repeat a run under a profiler)
+        from taufactor_gb300.autotune import apply
+        apply(s, args.tile, args.kmax)
+        tuning = {}
+    else:
+        tuning = {f"tile{t}_k{k}": round(ms, 5) for (t, k), ms in s.tune().items()}
     for _ in range(args.warmup):
         s.reset()
         s.solve(verbose=False, conv_crit=CONV_CRIT)
@@ -442,6 +447,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--tile", type=int, default=None, help="fixed tile shape instead of autotuning (0..2)")
+    ap.add_argument("--kmax", type=int, default=4, help="with --tile: half-sweeps per launch (1..4)")
     ap.add_argument("--profile", action="store_true", help="run the small profiler workload only")
     ap.add_argument("--batch", type=int, default=4, help="--profile: volumes")
     ap.add_argument("--side", type=int, default=256, help="--profile: volume side")
