@@ -271,6 +271,20 @@ int tf_kappa_pack(const tf_geom* g, const tf_operator* op, const float* kappa_de
 int tf_kappa_advance(const tf_geom* g, const tf_operator* op, float* field_dev, const float* kappa_split_dev,
                      const float* rhs_dev, int first_colour, int n_half, void* stream);
 
+/* The operator's faces for tf_kappa_advance_faces, computed once per kappa field (float32, the
+ * values the sweeps use; taufactor.py:586-603 with a per-voxel diffusivity): fx_dev holds
+ * batch * (nx + 1) planes of field_elems / (batch * nx) floats each (plane x + 1 = the face
+ * between x and x + 1, planes 0 and nx the Dirichlet faces of planes 0 and nx - 1), fy_dev,
+ * fz_dev and div_dev field_elems floats each (the +y and +z faces of every cell and the factor). */
+int tf_kappa_faces(const tf_geom* g, const float* kappa_split_dev, float* fx_dev, float* fy_dev, float* fz_dev,
+                   float* div_dev, void* stream);
+
+/* tf_kappa_advance from the packed faces: the same half-sweeps bit for bit, one division per
+ * voxel instead of six, float4 groups (every pointer 16-byte aligned). */
+int tf_kappa_advance_faces(const tf_geom* g, const tf_operator* op, float* field_dev, const float* fx_dev,
+                           const float* fy_dev, const float* fz_dev, const float* div_dev, const float* rhs_dev,
+                           int first_colour, int n_half, void* stream);
+
 /* Coefficients of the float64 steps below (coeff_f64): 0 = the sweeps' own float32 faces and
  * float32 diagonal (the reference's discrete operator, taufactor.py:577-603); 1 = float64 faces
  * 2ab/(a+b) of the float32 kappa values and the exact float64 diagonal, under which D_eff is a

@@ -25,6 +25,7 @@ EXPORTS = (
     "tf_batch_describe_rhs", "tf_batch_advance_rhs",
     "tf_batch_converge_static", "tf_kappa_pack", "tf_kappa_advance", "tf_kappa_layer_sums",
     "tf_kappa_residual_f64", "tf_kappa_adjoint_rhs", "tf_kappa_gradient", "tf_split_to_natural_f64",
+    "tf_kappa_faces", "tf_kappa_advance_faces",
 )
 TF_BATCH_ACTIVE, TF_BATCH_CONVERGED, TF_BATCH_NEEDS_HOST = 0, 1, 2
 
@@ -105,6 +106,8 @@ def load():
         "tf_batch_converge_static": (i32, [vp, vp, i32, i32, i64, i64, TfBatchState, C.c_double, i32, i32, vp]),
         "tf_kappa_pack": (i32, [G, O, vp, vp, vp, vp, vp]),
         "tf_kappa_advance": (i32, [G, O, vp, vp, vp, i32, i32, vp]),
+        "tf_kappa_faces": (i32, [G, vp, vp, vp, vp, vp, vp]),
+        "tf_kappa_advance_faces": (i32, [G, O, vp, vp, vp, vp, vp, vp, i32, i32, vp]),
         "tf_kappa_layer_sums": (i32, [G, vp, i32, i32, vp, vp, vp, vp]),
         "tf_kappa_residual_f64": (i32, [G, O, vp, vp, vp, i32, vp, vp, vp, vp]),
         "tf_kappa_adjoint_rhs": (i32, [G, vp, vp, C.c_double, i32, vp]),

@@ -7,7 +7,11 @@
 // layout (ghost cells 0 on closed faces, wrapped copies on periodic ones). With
 // kappa = D[label] every face, factor and update equals MultiPhaseSolver's bit for bit.
 //
-// k_kappa_sweep      one half-sweep in place (float4 groups of one colour), optional RHS
+// k_kappa_sweep      one half-sweep in place (one thread per voxel of one colour), optional RHS
+// k_kappa_face_pack  the operator's faces and factor, once per kappa field
+// k_kappa_sweep4     one half-sweep in place from the packed faces (float4 groups of one
+//                    colour, one division per voxel), optional RHS; the same bits as
+//                    k_kappa_sweep
 // k_kappa_residual   float64 r = b - A c with an explicit float64 right-hand side or the
 //                    Dirichlet terms; per-plane sums of r^2 and b^2
 //
@@ -140,6 +144,100 @@ __global__ void __launch_bounds__(256) k_kappa_sweep(float* __restrict__ c, cons
     s = __fadd_rn(s, __fmul_rn(cb[v.off(x, y, z - 1)], f.zm));
     if (rhs) s = __fadd_rn(s, rhs[b0 + o]);
     cb[o] = sor_finish(cb[o], quotient(s, f.div), a.omega);
+}
+
+// Packed faces, in the float32 values the sweeps use. hface(a, b) == hface(b, a) bit for bit
+// ((2a) b and (2b) a are the same rounded product), so a face is stored once and read by both
+// of its voxels.
+//   fx [b][x'][plane], x' = 0..NX: x' = x + 1 holds the face between planes x and x + 1; x' = 0
+//      and x' = NX hold the Dirichlet faces hface(k, k) of planes 0 and NX - 1
+//   fy [b][x][Y][...]: the face between padded rows Y and Y + 1 (0 past the last padded row)
+//   fz [b][x][Y][q][jp]: the face between cell z = 2 (jp - HJ) + q and z + 1 (0 past the row)
+//   dv [b][x][Y][q][jp]: the factor of kappa_faces for interior cells, inf elsewhere
+__global__ void k_kappa_face_pack(const float* __restrict__ kp, float* __restrict__ fx, float* __restrict__ fy,
+                                  float* __restrict__ fz, float* __restrict__ dv, const Geo g) {
+    const int pos = blockIdx.x * blockDim.x + threadIdx.x;  // q * ZH + jp
+    if (pos >= 2 * g.ZH) return;
+    const int Y = blockIdx.y;
+    const int bx = blockIdx.z;  // b * NX + x
+    const int x = bx % g.NX, b = bx / g.NX;
+    const int q = pos >= g.ZH ? 1 : 0;
+    const int jp = pos - q * g.ZH;
+    const long long o = (long long)bx * g.plane_f + (long long)Y * g.row_f + pos;
+    const float kc = kp[o];
+    fy[o] = Y + 1 < g.YP ? hface(kc, kp[o + g.row_f]) : 0.0f;
+    const long long on = q == 0 ? o + g.ZH : (jp + 1 < g.ZH ? o - g.ZH + 1 : -1);
+    fz[o] = on >= 0 ? hface(kc, kp[on]) : 0.0f;
+    const long long fxo = ((long long)b * (g.NX + 1) + x) * g.plane_f + (long long)Y * g.row_f + pos;
+    fx[fxo + g.plane_f] = x + 1 < g.NX ? hface(kc, kp[o + g.plane_f]) : hface(kc, kc);
+    if (x == 0) fx[fxo] = hface(kc, kc);
+    const int y = Y - HY, z = 2 * (jp - HJ) + q;
+    float d = __int_as_float(0x7f800000);
+    if (y >= 0 && y < g.NY && jp >= HJ && z < g.NZ) {
+        const KView v{g};
+        d = kappa_faces(kp + (long long)b * g.vol_f, v, x, y, z, kc).div;
+    }
+    dv[o] = d;
+}
+
+// One half-sweep in place from the packed faces: one thread per float4 group of the colour's
+// half-row (the arithmetic of k_kappa_sweep, taufactor.py:607-612).
+template <bool RHS>
+__global__ void __launch_bounds__(256) k_kappa_sweep4(float* __restrict__ c, const float* __restrict__ fx,
+                                                      const float* __restrict__ fy, const float* __restrict__ fz,
+                                                      const float* __restrict__ dv, const SweepArgs a, int colour) {
+    const Geo& g = a.g;
+    const int gmax = (half_len(g.NZ, 0) + 3) >> 2;
+    const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+    if (gi >= gmax) return;
+    const int y = blockIdx.y;
+    const int bx = blockIdx.z;  // b * NX + x
+    const int x = bx % g.NX, b = bx / g.NX;
+    const int q = (x + y + colour) & 1;
+    const int nj = half_len(g.NZ, q);
+    const int j = 4 * gi;
+    if (j >= nj) return;
+    const long long base = (long long)bx * g.plane_f + (long long)(y + HY) * g.row_f;
+    const long long rq = base + q * g.ZH + HJ + j;        // this group
+    const long long ro = base + (q ^ 1) * g.ZH + HJ + j;  // the other half-row, same j
+    const float4 cc = ld4(c + rq);
+    const float4 xp = x + 1 < g.NX ? ld4(c + rq + g.plane_f) : make_float4(a.ghi, a.ghi, a.ghi, a.ghi);
+    const float4 xm = x > 0 ? ld4(c + rq - g.plane_f) : make_float4(a.glo, a.glo, a.glo, a.glo);
+    const float4 yp = ld4(c + rq + g.row_f);
+    const float4 ym = ld4(c + rq - g.row_f);
+    float4 zp, zm;
+    z_neighbours(q, ld4(c + ro), q ? c[ro + 4] : c[ro - 1], zp, zm);
+    const long long fxq = ((long long)b * (g.NX + 1) + x) * g.plane_f + (long long)(y + HY) * g.row_f + q * g.ZH +
+                          HJ + j;  // fx plane x: the face between x - 1 and x
+    const float4 fxm = ld4(fx + fxq), fxp = ld4(fx + fxq + g.plane_f);
+    const float4 fyp = ld4(fy + rq), fym = ld4(fy + rq - g.row_f);
+    const float4 fzp = ld4(fz + rq);
+    float4 fzm;  // the face between z - 1 and z, stored at cell z - 1
+    if (q) {
+        fzm = ld4(fz + ro);
+    } else {
+        const float4 fo = ld4(fz + ro);
+        fzm = make_float4(fz[ro - 1], fo.x, fo.y, fo.z);
+    }
+    const float4 d = ld4(dv + rq);
+    float4 rv = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (RHS) rv = ld4(a.rhs + rq);
+    float4 nv;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        float s = __fadd_rn(__fmul_rn(comp(xp, i), comp(fxp, i)), __fmul_rn(comp(xm, i), comp(fxm, i)));
+        s = __fadd_rn(s, __fmul_rn(comp(yp, i), comp(fyp, i)));
+        s = __fadd_rn(s, __fmul_rn(comp(ym, i), comp(fym, i)));
+        s = __fadd_rn(s, __fmul_rn(comp(zp, i), comp(fzp, i)));
+        s = __fadd_rn(s, __fmul_rn(comp(zm, i), comp(fzm, i)));
+        if (RHS) s = __fadd_rn(s, comp(rv, i));
+        set_comp(nv, i, sor_finish(comp(cc, i), quotient(s, comp(d, i)), a.omega));
+    }
+    float* dst = c + rq;
+    if (j + 4 <= nj)
+        st4(dst, nv);
+    else
+        for (int i = 0; i < nj - j; ++i) dst[i] = comp(nv, i);
 }
 
 // float64 residual; bsrc (float64, split layout) replaces the Dirichlet terms when non-null.
@@ -406,6 +504,47 @@ int tf_kappa_advance(const tf_geom* g, const tf_operator* op, float* field_dev, 
     for (int i = 0; i < n_half; ++i, colour ^= 1) {
         SweepArgs a = make_args(geo, *op, field_dev, colour, 1, nullptr);
         k_kappa_sweep<<<grid, 256, 0, st>>>(field_dev, kappa_split_dev, rhs_dev, a, colour);
+        note_launch();
+        if (cudaGetLastError() != cudaSuccess) return TF_ERR_CUDA;
+        if (op->periodic) {
+            const int rc = refresh_ghosts(*g, op->periodic, field_dev, st);
+            if (rc) return rc;
+        }
+    }
+    return TF_OK;
+}
+
+int tf_kappa_faces(const tf_geom* g, const float* kappa_split_dev, float* fx_dev, float* fy_dev, float* fz_dev,
+                   float* div_dev, void* stream) {
+    if (!g || !kappa_split_dev || !fx_dev || !fy_dev || !fz_dev || !div_dev) return TF_ERR_ARG;
+    const Geo geo = make_geo(*g);
+    dim3 grid((2 * g->zh + 127) / 128, g->yp, g->batch * g->nx);
+    k_kappa_face_pack<<<grid, 128, 0, (cudaStream_t)stream>>>(kappa_split_dev, fx_dev, fy_dev, fz_dev, div_dev, geo);
+    note_launch();
+    return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
+}
+
+int tf_kappa_advance_faces(const tf_geom* g, const tf_operator* op, float* field_dev, const float* fx_dev,
+                           const float* fy_dev, const float* fz_dev, const float* div_dev, const float* rhs_dev,
+                           int first_colour, int n_half, void* stream) {
+    if (!g || !op || !field_dev || !fx_dev || !fy_dev || !fz_dev || !div_dev || n_half < 0) return TF_ERR_ARG;
+    const uintptr_t al = reinterpret_cast<uintptr_t>(field_dev) | reinterpret_cast<uintptr_t>(fx_dev) |
+                         reinterpret_cast<uintptr_t>(fy_dev) | reinterpret_cast<uintptr_t>(fz_dev) |
+                         reinterpret_cast<uintptr_t>(div_dev) | reinterpret_cast<uintptr_t>(rhs_dev);
+    if (al & 15) return TF_ERR_ARG;  // float4 loads
+    cudaStream_t st = (cudaStream_t)stream;
+    const Geo geo = make_geo(*g);
+    const int gmax = (half_len(g->nz, 0) + 3) >> 2;
+    const int bs = gmax >= 128 ? 128 : (gmax >= 32 ? 64 : 32);
+    dim3 grid((gmax + bs - 1) / bs, g->ny, g->batch * g->nx);
+    int colour = first_colour & 1;
+    for (int i = 0; i < n_half; ++i, colour ^= 1) {
+        SweepArgs a = make_args(geo, *op, field_dev, colour, 1, nullptr);
+        a.rhs = rhs_dev;
+        if (rhs_dev)
+            k_kappa_sweep4<true><<<grid, bs, 0, st>>>(field_dev, fx_dev, fy_dev, fz_dev, div_dev, a, colour);
+        else
+            k_kappa_sweep4<false><<<grid, bs, 0, st>>>(field_dev, fx_dev, fy_dev, fz_dev, div_dev, a, colour);
         note_launch();
         if (cudaGetLastError() != cudaSuccess) return TF_ERR_CUDA;
         if (op->periodic) {

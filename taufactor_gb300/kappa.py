@@ -99,6 +99,15 @@ class KappaSolver:
             prof = torch.linspace(self.top_bc + sh, self.bot_bc - sh, self.Nx, dtype=torch.float32).to(self.device)
             check(lib.tf_kappa_pack(C.byref(g), C.byref(op), _ptr(self.kappa), _ptr(prof), _ptr(self._ks),
                                     _ptr(self._c), st), "tf_kappa_pack")
+            # the operator's faces and factor, once: the sweeps then divide once per voxel
+            plane = g.field_elems // (self.batch_size * self.Nx)
+            f32 = dict(dtype=torch.float32, device=self.device)
+            self._fx = torch.empty(self.batch_size * (self.Nx + 1) * plane, **f32)
+            self._fy = torch.empty(g.field_elems, **f32)
+            self._fz = torch.empty(g.field_elems, **f32)
+            self._dv = torch.empty(g.field_elems, **f32)
+            check(lib.tf_kappa_faces(C.byref(g), _ptr(self._ks), _ptr(self._fx), _ptr(self._fy), _ptr(self._fz),
+                                     _ptr(self._dv), st), "tf_kappa_faces")
             self._flux = torch.empty((self.batch_size, self.Nx - 1), dtype=torch.float64, device=self.device)
             self._csum = torch.empty((self.batch_size, self.Nx), dtype=torch.float64, device=self.device)
         self._c64 = None
@@ -114,10 +123,11 @@ class KappaSolver:
 
     # ---------------------------------------------------------------- forward
     def _advance(self, n: int, field: torch.Tensor, rhs=None, op=None, first_colour=None):
-        check(self._lib.tf_kappa_advance(C.byref(self._geom), C.byref(op or self._op), _ptr(field), _ptr(self._ks),
-                                         _ptr(rhs) if rhs is not None else None,
-                                         self.iter % 2 if first_colour is None else first_colour, n,
-                                         self._stream()), "tf_kappa_advance")
+        check(self._lib.tf_kappa_advance_faces(C.byref(self._geom), C.byref(op or self._op), _ptr(field),
+                                               _ptr(self._fx), _ptr(self._fy), _ptr(self._fz), _ptr(self._dv),
+                                               _ptr(rhs) if rhs is not None else None,
+                                               self.iter % 2 if first_colour is None else first_colour, n,
+                                               self._stream()), "tf_kappa_advance_faces")
 
     def _layer_means(self):
         f, is64 = (self._c64, 1) if self._c64 is not None else (self._c, 0)
