@@ -363,6 +363,77 @@ def uneven_batch(dev, conv_crit=CONV_CRIT, repeat=2, refine_tols=(1e-8,)):
             "timing": "wall clock excl. input generation and solver construction"}
 
 
+def design_loop(dev, side=768, steps=50, lr=0.05, lam=0.5, tol=1e-8, conv_crit=1e-3):
+    """Gradient-driven design loop on one side^3 volume: kappa = sigmoid(logits), logits =
+    blur_sigma4(N(0,1)) from default_rng(5000); Adam on the logits maximising
+    D_eff - lam * mean(kappa). Every step: forward solve warm-started from the previous step's
+    field, FP64 refinement to a relative residual of tol, adjoint solve warm-started from the
+    previous adjoint field. Reports per-step times, the solve and adjoint residuals, Euler's
+    identity sum(kappa dD/dkappa) = D_eff per step and, at the last step, a directional central
+    difference along the update direction."""
+    import torch
+    from scipy.ndimage import gaussian_filter
+
+    import taufactor_gb300 as tg
+
+    logits0 = gaussian_filter(np.random.default_rng(5000).standard_normal((side,) * 3, dtype=np.float32), 4.0)
+    logits = torch.from_numpy(logits0.astype(np.float32)).to(dev).requires_grad_(True)
+    opt = torch.optim.Adam([logits], lr=lr, maximize=True)
+    prev = None
+    rows = []
+    t_all = time.perf_counter()
+    for k in range(steps):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        with torch.no_grad():
+            kap = torch.sigmoid(logits).float().contiguous()
+        s = tg.KappaSolver(kap, device=dev)
+        if prev is not None:
+            s.warm_start(prev)
+        s.solve(conv_crit=conv_crit, refine={"tol": tol, "max_outer": 40})
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        g = s.gradient(tol=tol, max_outer=40, lam0=prev.lam if prev is not None else None)[0]
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        d = float(s.D_eff[0])
+        euler = abs(float((s.kappa[0].double() * g).sum()) - d) / d
+        with torch.no_grad():
+            kk = kap.double()
+            logits.grad = ((g - lam / kap.numel()) * kk * (1.0 - kk)).float()
+        opt.step()
+        rows.append({"step": k, "forward_s": t1 - t0, "adjoint_s": t2 - t1, "half_sweeps": s.iter, "D_eff": d,
+                     "mean_kappa": float(kap.double().mean()), "objective": d - lam * float(kap.double().mean()),
+                     "fp64_residual": s.residual_history[-1], "adjoint_residual": s.adjoint_history[-1],
+                     "euler_rel_err": euler})
+        if prev is not None:
+            del prev
+        prev = s
+    total = time.perf_counter() - t_all
+    # directional central difference of D_eff along the last gradient direction at the last kappa
+    with torch.no_grad():
+        kap = prev.kappa[0]
+        direc = torch.sign(g).float()
+        h = 1e-3
+
+        def deff(kk):
+            t = tg.KappaSolver(kk.contiguous(), device=dev)
+            t.warm_start(prev)
+            t.solve(conv_crit=conv_crit, refine={"tol": 1e-13, "max_outer": 40})
+            return float(t.D_eff[0])
+
+        kp = (kap + h * direc).float()
+        km = (kap - h * direc).float()
+        fd = (deff(kp) - deff(km)) / 2.0
+        step = ((kp.double() - km.double()) / 2.0)
+        ad = float((g * step).sum())
+    return {"workload": f"design loop {side}^3, kappa = sigmoid(logits), logits = blur_sigma4(N(0,1)) rng 5000, "
+                        f"Adam lr {lr} on D_eff - {lam} mean(kappa)", "steps": steps, "total_s": total,
+            "mean_step_s": total / steps, "first": rows[0], "last": rows[-1],
+            "max_euler_rel_err": max(r["euler_rel_err"] for r in rows),
+            "direction_fd_rel_err": abs(fd - ad) / abs(fd), "fd_h": h, "per_step": rows}
+
+
 def adjoint_cost(dev, side=320, fd_voxels=0, tol=1e-12, fd_tol=1e-14):
     """Per-voxel conductivity kappa = sigmoid(blur_2(2 N(0,1))) on side^3 (default_rng(3003)):
     forward solve + FP64 refinement, then the adjoint gradient; times and, with fd_voxels > 0,
@@ -454,10 +525,12 @@ def main():
     ap.add_argument("--side", type=int, default=256, help="--profile: volume side")
     ap.add_argument("--half-sweeps", type=int, default=40, help="--profile: half-sweeps")
     ap.add_argument("--periodic", action="store_true", help="--profile: PeriodicSolver")
-    ap.add_argument("--workload", choices=["uneven", "adjoint"], default=None,
+    ap.add_argument("--workload", choices=["uneven", "adjoint", "design"], default=None,
                     help="print the secondary measurement of this workload only")
     ap.add_argument("--fd-voxels", type=int, default=0, help="--workload adjoint: finite-difference check")
     ap.add_argument("--adj-side", dest="adj_side", type=int, default=320, help="--workload adjoint: volume side")
+    ap.add_argument("--design-side", type=int, default=768, help="--workload design: volume side")
+    ap.add_argument("--design-steps", type=int, default=50, help="--workload design: Adam steps")
     args = ap.parse_args()
     if args.workload:
         import torch
@@ -465,6 +538,8 @@ def main():
         dev = torch.device("cuda", 0)
         if args.workload == "uneven":
             print(json.dumps(uneven_batch(dev)), flush=True)
+        elif args.workload == "design":
+            print(json.dumps(design_loop(dev, args.design_side, args.design_steps)), flush=True)
         else:
             print(json.dumps(adjoint_cost(dev, args.adj_side, args.fd_voxels)), flush=True)
     elif args.profile:

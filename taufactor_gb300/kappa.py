@@ -221,8 +221,11 @@ class KappaSolver:
         return self.residual_history
 
     # ---------------------------------------------------------------- adjoint
-    def gradient(self, tol: float = 1e-11, max_outer: int = 12, inner_half_sweeps=None) -> torch.Tensor:
-        """dD_eff/dkappa [B,X,Y,Z] (float64, on the device) at the current (refined) solution."""
+    def gradient(self, tol: float = 1e-11, max_outer: int = 12, inner_half_sweeps=None, lam0=None) -> torch.Tensor:
+        """dD_eff/dkappa [B,X,Y,Z] (float64, on the device) at the current (refined) solution.
+
+        lam0: optional starting adjoint field (another solver's `lam` of the same shape, e.g. the
+        previous step of a design loop); the adjoint field is kept as `lam`."""
         if self._c64 is None:
             self.refine(tol=tol)
         t0 = timer()
@@ -233,8 +236,14 @@ class KappaSolver:
             dj = torch.zeros(g.field_elems, dtype=torch.float64, device=self.device)
             check(lib.tf_kappa_adjoint_rhs(C.byref(g), _ptr(self._ks), _ptr(dj), float(scale), self._coeff64, st),
                   "tf_kappa_adjoint_rhs")
-            lam = torch.zeros(g.field_elems, dtype=torch.float64, device=self.device)
+            if lam0 is not None:
+                if lam0.numel() != g.field_elems:
+                    raise ValueError("lam0 must come from a solver of the same shape")
+                lam = lam0.to(device=self.device, dtype=torch.float64).clone()
+            else:
+                lam = torch.zeros(g.field_elems, dtype=torch.float64, device=self.device)
             self.adjoint_history = self._fp64_solve(lam, dj, tol, max_outer, n_inner)
+            self.lam = lam
             grad = torch.empty((self.batch_size, self.Nx, self.Ny, self.Nz), dtype=torch.float64, device=self.device)
             check(lib.tf_kappa_gradient(C.byref(g), C.byref(self._op), _ptr(self._c64), _ptr(lam), _ptr(self._ks),
                                         _ptr(grad), float(scale), float(self.top_bc), float(self.bot_bc), st),
