@@ -220,8 +220,10 @@ int tf_batch_advance_rhs(const void* desc_dev, const int32_t* work_dev, int n_wo
                          int launch, void* stream);
 
 /* Advance every active volume by the batch's half-sweeps per launch (colour 0 first, so the
- * completed half-sweeps must stay a multiple of it). work_dev: int32 pairs (volume, tile) with
- * tile = ty * tiles_z + tz. parity 0 reads buffers A and writes B, 1 the reverse. */
+ * completed half-sweeps must stay a multiple of it). work_dev: int32 quads (volume, tile, x0, x1)
+ * with tile = ty * tiles_z + tz: the CTA writes planes [x0, x1) of that tile column (items of
+ * one column must cover [0, nx) without overlap). parity 0 reads buffers A and writes B, 1 the
+ * reverse. */
 int tf_batch_advance(const void* desc_dev, const int32_t* work_dev, int n_work, const int32_t* status_dev,
                      int parity, void* stream);
 

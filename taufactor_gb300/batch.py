@@ -34,6 +34,7 @@ from .percolation import spans_x
 from .solvers import layer_metrics
 
 INTERVAL = 100  # half-sweeps between convergence checks (taufactor.py:184-185)
+CHUNK = 32  # planes per work item of the batched sweep
 
 
 def _ptr(t: torch.Tensor) -> int:
@@ -132,7 +133,11 @@ class BatchSolve:
                 self.fb.append(fb)
                 self.codes.append(code)
                 tiles = ((ny + ty.value - 1) // ty.value) * ((nz + tz.value - 1) // tz.value)
-                work += [(v, t) for t in range(tiles)]
+                # x-chunks of about CHUNK planes: items of large and small volumes take about
+                # equally long, so a launch does not wait on the longest columns
+                nch = max(1, round(nx / CHUNK))
+                bounds = [(c * nx) // nch for c in range(nch + 1)]
+                work += [(v, t, bounds[c], bounds[c + 1]) for t in range(tiles) for c in range(nch)]
                 planes += [(v, x) for x in range(nx)]
                 flux_off.append(nf)
                 csum_off.append(nc)

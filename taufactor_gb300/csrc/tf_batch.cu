@@ -4,8 +4,9 @@
 // memory holds, per volume, the TMA tensor maps of its two field buffers and its codes, the
 // sweep arguments for both ping-pong directions and the offsets of its layer sums. One
 // k_stream_multi launch advances every still-active volume by K half-sweeps: CTA w takes work
-// item (volume, tile) from a table and runs the same per-tile body as the single-volume
-// kernel; CTAs of volumes whose status is not "active" return at once. k_layer_sums_multi and
+// item (volume, tile, x0, x1) from a table and runs the same per-tile body as the single-volume
+// kernel on planes [x0, x1) of that tile column (x-chunks keep the items of large and small
+// volumes about equally long); CTAs of volumes whose status is not "active" return at once. k_layer_sums_multi and
 // k_batch_check then evaluate the reference's convergence rule (taufactor.py:109-153,
 // :293-331) per volume on the device and set its status, so a whole check interval -- sweeps,
 // layer sums, decision -- runs without the host and can be captured in a CUDA graph.
@@ -37,26 +38,26 @@ struct alignas(64) VolDesc {
 };
 
 __global__ void __launch_bounds__(BShape::NT, 2)
-    k_stream_multi(const VolDesc* __restrict__ desc, const int2* __restrict__ work,
+    k_stream_multi(const VolDesc* __restrict__ desc, const int4* __restrict__ work,
                    const int32_t* __restrict__ status, int parity) {
     extern __shared__ __align__(128) unsigned char smem[];
-    const int2 item = work[blockIdx.x];
+    const int4 item = work[blockIdx.x];
     const int v = item.x;
     if (status[v] != TF_BATCH_ACTIVE) return;
     const VolDesc* d = desc + v;
     const int tz = item.y % d->tiles_z, ty = item.y / d->tiles_z;
     const SweepArgs a = parity ? d->ba : d->ab;
     stream_tile<TF_KIND_BINARY, BTY, BTZ, BK, false>(parity ? &d->map_b : &d->map_a, &d->map_c, a, nullptr,
-                                                     tz * (BTZ / 2), ty * BTY, 0, 0, a.g.NX, smem);
+                                                     tz * (BTZ / 2), ty * BTY, 0, item.z, item.w, smem);
 }
 
 // Correction sweeps: launch `launch` of an inner solve; volume v takes part while
 // launch < launches[v] (an even count, so each volume's result ends in buffer A).
 __global__ void __launch_bounds__(BShape::NT, 2)
-    k_stream_multi_rhs(const VolDesc* __restrict__ desc, const int2* __restrict__ work,
+    k_stream_multi_rhs(const VolDesc* __restrict__ desc, const int4* __restrict__ work,
                        const int32_t* __restrict__ launches, int launch) {
     extern __shared__ __align__(128) unsigned char smem[];
-    const int2 item = work[blockIdx.x];
+    const int4 item = work[blockIdx.x];
     const int v = item.x;
     if (launch >= launches[v]) return;
     const VolDesc* d = desc + v;
@@ -64,7 +65,7 @@ __global__ void __launch_bounds__(BShape::NT, 2)
     const int parity = launch & 1;
     const SweepArgs a = parity ? d->ba : d->ab;
     stream_tile<TF_KIND_BINARY, BTY, BTZ, BK, true>(parity ? &d->map_b : &d->map_a, &d->map_c, a, nullptr,
-                                                    tz * (BTZ / 2), ty * BTY, 0, 0, a.g.NX, smem);
+                                                    tz * (BTZ / 2), ty * BTY, 0, item.z, item.w, smem);
 }
 
 // One CTA per (volume, plane): float64 sums of the masked x-flux through face x|x+1 and of the
@@ -240,7 +241,7 @@ int tf_batch_advance_rhs(const void* desc_dev, const int32_t* work_dev, int n_wo
                          int launch, void* stream) {
     if (!desc_dev || !work_dev || n_work <= 0 || !launches_dev || launch < 0) return TF_ERR_ARG;
     k_stream_multi_rhs<<<n_work, BShape::NT, BShape::SMEM, (cudaStream_t)stream>>>(
-        static_cast<const VolDesc*>(desc_dev), reinterpret_cast<const int2*>(work_dev), launches_dev, launch);
+        static_cast<const VolDesc*>(desc_dev), reinterpret_cast<const int4*>(work_dev), launches_dev, launch);
     note_launch();
     return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
 }
@@ -249,7 +250,7 @@ int tf_batch_advance(const void* desc_dev, const int32_t* work_dev, int n_work, 
                      int parity, void* stream) {
     if (!desc_dev || !work_dev || n_work <= 0 || !status_dev) return TF_ERR_ARG;
     k_stream_multi<<<n_work, BShape::NT, BShape::SMEM, (cudaStream_t)stream>>>(
-        static_cast<const VolDesc*>(desc_dev), reinterpret_cast<const int2*>(work_dev), status_dev, parity & 1);
+        static_cast<const VolDesc*>(desc_dev), reinterpret_cast<const int4*>(work_dev), status_dev, parity & 1);
     note_launch();
     return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
 }

@@ -38,6 +38,26 @@ def test_batch_matches_single_volume_solvers(graph):
         assert np.array_equal(got, want), v
 
 
+def test_batch_x_chunks_match_single_volume_solvers(monkeypatch):
+    """Work items that cover tile columns in several x-chunks (20 planes each here) give the
+    single-volume results bit for bit, also with the FP64 correction."""
+    import taufactor_gb300.batch as batch_mod
+
+    monkeypatch.setattr(batch_mod, "CHUNK", 20)
+    vols, periodic = _volumes()
+    b = tg.BatchSolve(vols, periodic=periodic)
+    assert b.n_work > sum(((s[1] + 15) // 16) * ((s[2] + 63) // 64) for s in SHAPES)
+    res = b.solve(conv_crit=1e-3)
+    for v, (img, per) in enumerate(zip(vols, periodic)):
+        s = (tg.PeriodicSolver if per else tg.Solver)(img)
+        s.solve(verbose=False, conv_crit=1e-3)
+        assert res[v].iter == s.iter
+        np.testing.assert_allclose(res[v].D_eff, s.D_eff, rtol=1e-12)
+        assert np.array_equal(b.field(v).cpu().numpy()[:, :, 1:-1, 1:-1], s.field.cpu().numpy()[:, :, 1:-1, 1:-1])
+    res = b.refine(tol=1e-10)
+    assert all(r.residual_history[-1] < 1e-10 for r in res)
+
+
 def test_batch_non_percolating_volume():
     vols, periodic = _volumes()
     dead = np.zeros((20, 16, 32), dtype=np.uint8)
