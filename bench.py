@@ -449,6 +449,9 @@ def adjoint_cost(dev, side=320, fd_voxels=0, tol=1e-12, fd_tol=1e-14):
 
     import taufactor_gb300 as tg
 
+    warm = tg.KappaSolver(np.full((32, 32, 32), 0.5, dtype=np.float32), device=dev)  # first-call costs
+    warm.solve(conv_crit=1e-3, refine={"tol": tol})
+    warm.gradient(tol=tol)
     logits = gaussian_filter(2.0 * np.random.default_rng(3003).standard_normal((side,) * 3, dtype=np.float32), 2.0)
     kap = (1.0 / (1.0 + np.exp(-logits))).astype(np.float32)
     s = tg.KappaSolver(kap, device=dev)
@@ -467,6 +470,43 @@ def adjoint_cost(dev, side=320, fd_voxels=0, tol=1e-12, fd_tol=1e-14):
            "D_eff": float(s.D_eff[0]),
            # D_eff is homogeneous of degree 1 in kappa, so sum(kappa * dD_eff/dkappa) = D_eff
            "euler_rel_err": abs(float((s.kappa.double() * g).sum()) - float(s.D_eff[0])) / float(s.D_eff[0])}
+    # per-phase gradients of MultiPhaseSolver on the three-label volume (labels = argmax of three
+    # blurred fields, default_rng(3000..3002), D = {0: 0, 1: 1, 2: 0.1}) against central
+    # differences in D_1 and D_2 of the operator they differentiate: kappa = D[label] with float64
+    # faces (the float32 faces of MultiPhaseSolver's own refined D_eff move in rounding steps that
+    # dominate a difference of step 1e-3). D_0 = 0 is a one-sided point: a phase of zero
+    # conductivity is not part of the system, so no central difference exists there.
+    from taufactor_gb300.synthetic import three_phase
+
+    lab = three_phase(side)
+    ds = {0: 0.0, 1: 1.0, 2: 0.1}
+    m = tg.MultiPhaseSolver(lab, dict(ds), device=dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    m.solve(verbose=False, conv_crit=1e-3, refine={"tol": tol})
+    torch.cuda.synchronize()
+    t_mf = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    pg = m.phase_gradients(conv_crit=1e-3, tol=tol)
+    torch.cuda.synchronize()
+    t_pg = time.perf_counter() - t0
+    phase = {"forward_s": t_mf, "phase_gradients_s": t_pg, "D_eff": float(m.D_eff[0]),
+             "gradients": {str(p): float(v[0]) for p, v in pg.items()}}
+    for p in (1, 2):
+        h = 1e-3
+        dd = []
+        for sgn in (1, -1):
+            dsp = dict(ds)
+            dsp[p] = ds[p] + sgn * h
+            kp = np.asarray([dsp[0], dsp[1], dsp[2]], dtype=np.float32)[lab]
+            t = tg.KappaSolver(kp, device=dev)
+            t.warm_start(m.kappa_solver)
+            t.solve(conv_crit=1e-3, refine={"tol": fd_tol, "max_outer": 40})
+            dd.append(float(t.D_eff[0]))
+        hp = float(np.float32(ds[p] + h)) - float(np.float32(ds[p] - h))
+        fd = (dd[0] - dd[1]) / hp
+        phase[f"fd_rel_err_phase{p}"] = abs(fd - float(pg[p][0])) / abs(fd)
+    out["multiphase_320"] = phase
     if fd_voxels:
         def deff(kk):
             t = tg.KappaSolver(kk, device=dev)

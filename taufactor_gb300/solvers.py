@@ -587,7 +587,10 @@ class MultiPhaseSolver(ThroughTransportSolver):
 
         Builds the per-voxel field kappa = D[label] (float32, the same faces as this solver,
         bit for bit), solves it to the reference's rule plus FP64 defect correction, solves the
-        adjoint and sums dD_eff/dkappa over the voxels of each label. No reference counterpart
+        adjoint and sums dD_eff/dkappa over the voxels of each label. The derivative is that of
+        the operator with float64 faces 2ab/(a+b) (KappaSolver's default): with float32 faces
+        D_eff moves in rounding steps. For a label of conductivity 0 the value is not a
+        derivative (the label's voxels are outside the system there). No reference counterpart
         (the reference solve runs under no_grad, taufactor.py:172).
         """
         from .kappa import KappaSolver
