@@ -174,7 +174,7 @@ __device__ __forceinline__ void stream_tile(const CUtensorMap* tmf, const CUtens
     const int xs = x0 > K ? x0 - K : 0;
     const int xe = x1 + K < NX ? x1 + K : NX;
     auto issue = [&](int x) {
-        const int s = (x - xs) % NS;
+        const int s = (int)((unsigned)(x - xs) % NS);
         mbar_arrive_expect_tx(&bar[s], S::FBYTES + S::CBYTES);
         tma_load_3d(F0 + s * (S::SLOT / 4), tmf, &bar[s], j0, row0, b * NX + x);
         tma_load_3d(C0 + s * S::SLOT, tmc, &bar[s], j0, row0, b * NX + x);
@@ -210,8 +210,8 @@ __device__ __forceinline__ void stream_tile(const CUtensorMap* tmf, const CUtens
             if (t < total) {
                 if (tid == 0 && t + D < xe) issue(t + D);
                 if (t < xe) {
-                    const int slot = (t - xs) % NS;
-                    if (!mbar_wait_bounded(&bar[slot], ((t - xs) / NS) & 1)) *s_fail = 1;
+                    const int slot = (int)((unsigned)(t - xs) % NS);
+                    if (!mbar_wait_bounded(&bar[slot], ((unsigned)(t - xs) / NS) & 1)) *s_fail = 1;
                     const float* Fs = F0 + slot * (S::SLOT / 4);
                     const unsigned char* Cs = C0 + slot * S::SLOT;
                     const float4 e4 = ld4(Fs + (2 * ty) * WJ + jj);
@@ -240,8 +240,9 @@ __device__ __forceinline__ void stream_tile(const CUtensorMap* tmf, const CUtens
                     // rows [s, ROWS - s) form the region of half-sweep s: it shrinks by one row per
                     // half-sweep so the tile interior is exact after K of them
                     if (p >= xs && p < NX && (stage_rows & (1u << s))) {
-                        float* Fp = F0 + ((p - xs) % NS) * (S::SLOT / 4);
-                        const unsigned char* Cp = C0 + ((p - xs) % NS) * S::SLOT;
+                        const int ps = (int)((unsigned)(p - xs) % NS);  // p >= xs here
+                        float* Fp = F0 + ps * (S::SLOT / 4);
+                        const unsigned char* Cp = C0 + ps * S::SLOT;
                         const bool at_lo = p == 0, at_hi = p == NX - 1;
                         // global address of this thread's group in the right-hand side (padded
                         // coordinates; rows beyond the ghost bands and groups past the row read 0)
