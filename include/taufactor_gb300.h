@@ -40,6 +40,7 @@ extern "C" {
 #define TF_KIND_BINARY 0      /* Solver / PeriodicSolver: divisor = conductive-neighbour count  */
 #define TF_KIND_ANISOTROPIC 1 /* AnisotropicSolver: y, z neighbours weighted by ky, kz          */
 #define TF_KIND_MULTIPHASE 2  /* MultiPhaseSolver(s): harmonic-mean face conductances          */
+#define TF_KIND_ELECTRODE 3   /* ElectrodeSolver(s): binary neighbour sum, divisor nn + k0 * nr  */
 
 /* periodic flags */
 #define TF_PERIODIC_Y 1
@@ -93,10 +94,16 @@ int tf_geometry(int batch, int nx, int ny, int nz, int periodic, tf_geom* out);
  * :459-471), the label map of MultiPhaseSolver.init_conductive_neighbours (:585-592) and the
  * chequerboard (:218-225; colour is taken from the voxel index instead).
  *   phase_dev   uint8 [batch][nx][ny][nz] (natural layout). binary/anisotropic: 1 = conductive,
- *               0 = not; multiphase: phase index 1..n_phases.
+ *               0 = not; multiphase: phase index 1..n_phases; electrode: 1 = conductive,
+ *               2 = reactive, 0 = neither.
  *   profile_dev float [nx] initial value of a conductive voxel in plane x.
  *   code_dev    uint8 [code_bytes]: binary = neighbour count (0 = frozen), anisotropic =
- *               neighbour pattern index into op->divisor, multiphase = phase index.
+ *               neighbour pattern index into op->divisor, multiphase = phase index,
+ *               electrode = 1 + nn + 8 nr for conductive voxels (nn conductive neighbours, the
+ *               inlet face x = -1 counted twice and the outlet face x = nx closed; nr reactive
+ *               neighbours; taufactor/electrode.py:46-62) and 0 otherwise; the divisor of volume
+ *               b is nn + nr * op->divisor[b] in float32 (op->divisor[b] = k_0 of volume b,
+ *               taufactor.py:47-55), inf where 0.
  *   field_dev   float [field_elems]. Ghost cells are filled too. */
 int tf_pack(const tf_geom* g, const tf_operator* op, const uint8_t* phase_dev,
             const float* profile_dev, uint8_t* code_dev, float* field_dev, void* stream);
@@ -146,7 +153,10 @@ int tf_layer_sums_f64(const tf_geom* g, const tf_operator* op, const double* fie
  * Solver.vertical_flux / MultiPhaseSolver.vertical_flux (taufactor.py:412-419, :615-620) with
  * torch.mean(..., (2, 3)) (:296) and the c_x mean (:307).
  *   flux_sum_dev double [batch][nx-1]: sum over (y, z) of the x-flux through face x|x+1
- *   c_sum_dev    double [batch][nx]:   sum over (y, z) of the field in plane x  */
+ *   c_sum_dev    double [batch][nx]:   sum over (y, z) of the field in plane x
+ * TF_KIND_ELECTRODE: flux_sum_dev holds [batch][nx] sums of ElectrodeSolver's fluxes
+ * (taufactor/electrode.py:70-74): plane 0 (left_bc - c) / 0.5 with left_bc = ghost_lo / 2,
+ * plane x > 0 c[x-1] - c[x], each 0 where c or its x-1 neighbour is 0. */
 int tf_layer_sums(const tf_geom* g, const tf_operator* op, const float* field_dev,
                   const uint8_t* code_dev, double* flux_sum_dev, double* c_sum_dev, void* stream);
 

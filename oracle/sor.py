@@ -20,6 +20,10 @@ Everything here follows tldr-group/taufactor v1.2.1, ``taufactor/taufactor.py``:
                         periodic ghost copy :501-505, :652-656
 * flux / metrics        ``vertical_flux`` :412-419, :615-620; ``compute_metrics`` :293-331
 * convergence           ``SORSolver.check_convergence``            :109-153
+* electrode             ``ElectrodeSolver`` / ``PeriodicElectrodeSolver`` (taufactor/electrode.py:13-157):
+                        masks :36-40, cosh initial field :42-50, neighbour counts :52-62 and
+                        :135-150, reaction prefactor ``SORSolver.__init__`` :47-55, metrics :64-103;
+                        impedance ``compute_impedance_batched`` (taufactor/utils.py:75-98)
 
 The per-element float32 operation order is the reference's (left-to-right neighbour sums, one
 IEEE rounding per operation, no fused multiply-add), so a half-sweep here is bitwise equal to the
@@ -37,7 +41,8 @@ from .percolation import spans_axis0
 
 F32 = np.float32
 
-KINDS = ("binary", "periodic", "anisotropic", "multiphase", "periodic_multiphase", "kappa", "periodic_kappa")
+KINDS = ("binary", "periodic", "anisotropic", "multiphase", "periodic_multiphase", "kappa", "periodic_kappa",
+         "electrode", "periodic_electrode")
 
 
 def expand_to_4d(img) -> np.ndarray:
@@ -96,7 +101,8 @@ def _roll_sum(t: np.ndarray, weights=(1.0, 1.0, 1.0)) -> np.ndarray:
     return s
 
 
-def neighbour_counts(mask: np.ndarray, periodic: bool = False, weights=(1.0, 1.0, 1.0)) -> np.ndarray:
+def neighbour_counts(mask: np.ndarray, periodic: bool = False, weights=(1.0, 1.0, 1.0), xpad=(2.0, 2.0),
+                     zero_inf: bool = True) -> np.ndarray:
     """Conductive-neighbour count nn, inf where solid or nn == 0.
 
     Dirichlet x-faces count twice because the conductor boundary sits half a voxel away
@@ -104,7 +110,7 @@ def neighbour_counts(mask: np.ndarray, periodic: bool = False, weights=(1.0, 1.0
     variant weights y,z neighbours by (dx/dy)^2, (dx/dz)^2 (:459-471).
     """
     m = mask.astype(F32)
-    p = pad_volume(m, (2.0, 2.0))
+    p = pad_volume(m, xpad)
     if periodic:
         p = p[:, :, 1:-1, 1:-1]
         nn = _roll_sum(p, weights)[:, 1:-1]
@@ -112,8 +118,41 @@ def neighbour_counts(mask: np.ndarray, periodic: bool = False, weights=(1.0, 1.0
         nn = _roll_sum(p, weights)[:, 1:-1, 1:-1, 1:-1]
     nn = nn.copy()
     nn[m == 0] = np.inf
-    nn[nn == 0] = np.inf
+    if zero_inf:
+        nn[nn == 0] = np.inf
     return nn
+
+
+def electrode_prefactor(cond: np.ndarray, reac: np.ndarray, periodic: bool, dx: float):
+    """Reactive-neighbour counts (electrode.py:52-62 / :143-150) and the reference's float32
+    a_x [B,Nx], k_0 [B], vol_x [B,Nx] (taufactor.py:40-55). Computed with the same torch float32
+    operations as the reference, so k_0 agrees to the last bit."""
+    import torch
+
+    B, X, Y, Z = cond.shape
+    mask_t = torch.from_numpy(cond.astype(F32))
+    vol_x = torch.mean(mask_t, (2, 3))
+    r = torch.from_numpy(reac.astype(F32))
+    rp = torch.nn.functional.pad(r, (0, 0, 0, 0, 1, 1) if periodic else (1, 1, 1, 1, 1, 1))
+    s = torch.zeros_like(rp)
+    for dim in range(1, 4):
+        for dr in (1, -1):
+            s += torch.roll(rp, dr, dim)
+    reac_nn = s[:, 1:-1] if periodic else s[:, 1:-1, 1:-1, 1:-1]
+    reac_nn[~torch.from_numpy(cond)] = 0.0
+    a_x = torch.sum(reac_nn, (2, 3)) / (Y * Z * dx)
+    k_0 = torch.mean(vol_x, 1) / torch.mean(a_x * dx, 1) / X ** 2
+    return reac_nn.numpy(), a_x.numpy(), k_0.numpy(), vol_x.numpy()
+
+
+def compute_impedance_batched(R: np.ndarray, C: np.ndarray, freq: np.ndarray) -> np.ndarray:
+    """Transmission-line impedance [B,F] (taufactor/utils.py:75-98)."""
+    bs, nx = R.shape
+    w = freq[None, :].repeat(bs, axis=0) if freq.ndim == 1 else freq
+    Z = np.full_like(w, 1e50, dtype=complex)
+    for k in range(nx - 1, -1, -1):
+        Z = R[:, k][:, None] + 1.0 / (1j * w * C[:, k][:, None] + 1.0 / Z)
+    return Z
 
 
 def harmonic_mean(a: np.ndarray, b: np.ndarray) -> np.ndarray:
@@ -177,7 +216,7 @@ class OracleSolve:
     top_bc, bot_bc = -0.5, 0.5
 
     def __init__(self, img, kind="binary", omega=None, D_0=1.0, diffusivities=None,
-                 spacing=None):
+                 spacing=None, conductive_label=1, reactive_label=0):
         if kind not in KINDS:
             raise ValueError(f"unknown kind {kind}")
         self.kind = kind
@@ -186,9 +225,13 @@ class OracleSolve:
         if omega is None:
             omega = default_omega(self.Nx)
         self.omega = omega
-        self.periodic = kind in ("periodic", "periodic_multiphase", "periodic_kappa")
+        self.periodic = kind in ("periodic", "periodic_multiphase", "periodic_kappa", "periodic_electrode")
         self.multiphase = kind in ("multiphase", "periodic_multiphase", "kappa", "periodic_kappa")
+        self.electrode = kind in ("electrode", "periodic_electrode")
         img32 = self.cpu_img.astype(F32)
+        if self.electrode:
+            self._init_electrode(img32, omega, spacing, conductive_label, reactive_label)
+            return
         if kind in ("kappa", "periodic_kappa"):
             # per-voxel float32 diffusivity given directly (MultiPhaseSolver's map, :586-588)
             self.Ds = {}
@@ -239,6 +282,69 @@ class OracleSolve:
         self.converged = False
         self.old_tau = 0
         self.tau = self.tau_x = self.D_eff = None
+
+    def _init_electrode(self, img32, omega, spacing, cond_label, reac_label):
+        """ElectrodeSolver / PeriodicElectrodeSolver set-up (electrode.py:18-62, taufactor.py:40-55)."""
+        self.left_bc, self.electrode_bc = 1.0, 0.0
+        self.dx = spacing or 1
+        cond = img32 == F32(cond_label)
+        reac = (img32 == F32(reac_label)) & ~cond
+        mask = cond.astype(F32)
+        nn = neighbour_counts(mask, self.periodic, xpad=(2.0, 0.0), zero_inf=False)
+        reac_nn, self.a_x, self.k_0, self.vol_x = electrode_prefactor(cond, reac, self.periodic, self.dx)
+        factor = nn + reac_nn * self.k_0[:, None, None, None]
+        factor[factor == 0] = np.inf
+        self.factor = factor.astype(F32)
+        self.mask = mask
+        self.conductive_labels = [cond_label]
+        x = np.arange(self.Nx) + 0.5
+        c_init = self.electrode_bc + (self.left_bc - self.electrode_bc) * np.cosh(1 - x / self.Nx) / np.cosh(1)
+        vec = c_init.astype(F32)
+        self.field = pad_volume(mask * vec[None, :, None, None], (2 * self.left_bc, 0.0)).astype(F32)
+        self.cb = chequerboard((self.Nx, self.Ny, self.Nz), omega)
+        self.c_x = 0
+        self.iter = 0
+        self.converged = False
+        self.old_tau = 0
+        self.tau = self.tau_x = self.D_eff = None
+
+    def electrode_layer_means(self):
+        """float64 per-layer means of ElectrodeSolver's fluxes [B,Nx] and of the field [B,Nx]
+        (electrode.py:65, :70-74): plane 0 (left_bc - c)/0.5, plane x > 0 c[x-1] - c[x], 0 where
+        c or c[x-1] is 0."""
+        f = self.field
+        c = f[:, 1:-1, 1:-1, 1:-1]
+        cm = f[:, :-2, 1:-1, 1:-1]
+        fl = (-c + cm).astype(F32)
+        fl[:, 0] = (F32(self.left_bc) - c[:, 0]) / F32(0.5)
+        fl[c == 0] = 0
+        fl[cm == 0] = 0
+        return fl.astype(np.float64).mean(axis=(2, 3)), c.astype(np.float64).mean(axis=(2, 3))
+
+    def electrode_metrics(self):
+        """electrode.py:64-103 on the float64 layer means."""
+        fluxes, c_raw = self.electrode_layer_means()
+        vol_x = self.vol_x
+        c_x = np.divide(c_raw, vol_x, out=np.zeros(c_raw.shape), where=vol_x != 0)
+        rel = np.max(np.abs(c_x - self.c_x), axis=1)
+        self.c_x = c_x
+        f1 = np.concatenate((2 * (self.left_bc - c_x[:, :1]), (-c_x[:, 1:] + c_x[:, :-1])), axis=1)
+        f1[:, 1:][vol_x[:, 1:] == 0] = 0
+        f1[:, 1:][vol_x[:, :-1] == 0] = 0
+        eps = np.concatenate((vol_x[:, :1], 0.5 * (vol_x[:, :-1] + vol_x[:, 1:])), axis=1)
+        self.tau_x = np.divide(eps * f1, fluxes, out=np.full_like(f1, np.nan), where=fluxes != 0)
+        fluxes[:, :-1] -= fluxes[:, 1:]
+        self.k_x = np.divide(fluxes, c_x - self.electrode_bc, out=np.zeros_like(c_x),
+                             where=(c_x - self.electrode_bc) != 0) / self.k_0[:, None]
+        freq = np.mean(eps, axis=1, keepdims=True) / np.mean(self.a_x * self.dx, axis=1, keepdims=True) / self.Nx ** 2 * 2 ** -3
+        R = self.tau_x / eps
+        R[eps == 0] = 1e30
+        R[np.isnan(self.tau_x)] = 1e30
+        z_sim = compute_impedance_batched(R, self.a_x * self.dx, freq)
+        r_id = 1 / np.mean(eps, axis=1)[:, None].repeat(self.Nx, axis=1)
+        c_id = np.mean(self.a_x * self.dx, axis=1)[:, None].repeat(self.Nx, axis=1)
+        z_id = compute_impedance_batched(r_id, c_id, freq)
+        return z_sim[:, 0].real / z_id[:, 0].real, rel
 
     # -------------------------------------------------------------- half-sweep
     def apply_boundary_conditions(self):
@@ -302,6 +408,8 @@ class OracleSolve:
 
     def compute_metrics(self):
         """tau, relative error and D_eff from the layer fluxes (taufactor.py:293-331)."""
+        if self.electrode:
+            return self.electrode_metrics()
         self.flux_1d, c_x = self.layer_means()
         return metrics_from_layers(self, self.flux_1d, c_x)
 

@@ -2,15 +2,16 @@
 
 Drop-in for the through-transport solvers of tldr-group/taufactor v1.2.1
 (``taufactor/__init__.py:3-11``): ``Solver``, ``PeriodicSolver``, ``AnisotropicSolver``,
-``MultiPhaseSolver`` and ``PeriodicMultiPhaseSolver`` with the same constructor and ``solve()``
-surface. The sweeps run as hand-written CUDA kernels of ``lib/libtaufactor_gb300.so`` through
+``MultiPhaseSolver``, ``PeriodicMultiPhaseSolver``, ``ElectrodeSolver`` and
+``PeriodicElectrodeSolver`` with the same constructor and ``solve()`` surface. The sweeps run as hand-written CUDA kernels of ``lib/libtaufactor_gb300.so`` through
 its C ABI (``include/taufactor_gb300.h``).
 """
 from .batch import BatchSolve
 from .kappa import DeffFunction, KappaSolver, d_eff
-from .solvers import (AnisotropicSolver, MultiPhaseSolver, PeriodicMultiPhaseSolver, PeriodicSolver,
-                      SORSolver, Solver, ThroughTransportSolver)
+from .solvers import (AnisotropicSolver, ElectrodeSolver, MultiPhaseSolver, PeriodicElectrodeSolver,
+                      PeriodicMultiPhaseSolver, PeriodicSolver, SORSolver, Solver, ThroughTransportSolver)
 
 __all__ = ["Solver", "PeriodicSolver", "AnisotropicSolver", "MultiPhaseSolver", "PeriodicMultiPhaseSolver",
+           "ElectrodeSolver", "PeriodicElectrodeSolver",
            "SORSolver", "ThroughTransportSolver", "BatchSolve", "KappaSolver", "DeffFunction", "d_eff"]
 __version__ = "0.1.0"

@@ -13,6 +13,7 @@ _LIB_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lib", "lib
 TF_OK, TF_ERR_ARG, TF_ERR_CUDA, TF_ERR_TIMEOUT, TF_ERR_UNSUPPORTED, TF_ERR_NOTCONV = range(6)
 TF_KIND_BINARY, TF_KIND_ANISOTROPIC, TF_KIND_MULTIPHASE = 0, 1, 2
 TF_PERIODIC_Y, TF_PERIODIC_Z = 1, 2
+TF_KIND_ELECTRODE = 3
 TF_MAX_PHASES = 31
 TF_MAX_HALF_SWEEPS = 4
 

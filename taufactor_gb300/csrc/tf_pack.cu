@@ -30,11 +30,12 @@ __device__ __forceinline__ bool src_cell(const Geo& g, int periodic, int y, int 
     return true;
 }
 
-// value of the conductive mask at a neighbour (0 outside closed faces, wrapped on periodic)
-__device__ __forceinline__ int mask_at(const uint8_t* P, const Geo& g, int periodic, int x, int y, int z) {
+// value of the mask "phase == ph" at a neighbour (0 outside closed faces, wrapped on periodic)
+__device__ __forceinline__ int mask_at(const uint8_t* P, const Geo& g, int periodic, int x, int y, int z,
+                                       int ph = 1) {
     int ys, zs;
     if (!src_cell(g, periodic, y, z, ys, zs)) return 0;
-    return P[((long long)x * g.NY + ys) * g.NZ + zs] == 1;
+    return P[((long long)x * g.NY + ys) * g.NZ + zs] == ph;
 }
 
 __global__ void k_pack(const uint8_t* __restrict__ phase, const float* __restrict__ profile,
@@ -59,6 +60,21 @@ __global__ void k_pack(const uint8_t* __restrict__ phase, const float* __restric
         if (a.kind == TF_KIND_MULTIPHASE) {
             cd = (uint8_t)ph;
             fv = op.conductive[ph & 31] ? profile[x] : 0.0f;
+        } else if (ph == 1 && a.kind == TF_KIND_ELECTRODE) {
+            // taufactor/electrode.py:46-62: conductive neighbours with the mask padded 2 at the
+            // inlet and 0 at the (closed) outlet, reactive neighbours (phase 2) padded 0
+            const int per = a.periodic;
+            const long long ox = ((long long)x * g.NY + ys) * g.NZ + zs, sx = (long long)g.NY * g.NZ;
+            const int xm = x > 0 ? (P[ox - sx] == 1) : 2;
+            const int xp = x + 1 < g.NX ? (P[ox + sx] == 1) : 0;
+            const int nn = xm + xp + mask_at(P, g, per, x, ys - 1, zs) + mask_at(P, g, per, x, ys + 1, zs) +
+                           mask_at(P, g, per, x, ys, zs - 1) + mask_at(P, g, per, x, ys, zs + 1);
+            const int rxm = x > 0 ? (P[ox - sx] == 2) : 0;
+            const int rxp = x + 1 < g.NX ? (P[ox + sx] == 2) : 0;
+            const int nr = rxm + rxp + mask_at(P, g, per, x, ys - 1, zs, 2) + mask_at(P, g, per, x, ys + 1, zs, 2) +
+                           mask_at(P, g, per, x, ys, zs - 1, 2) + mask_at(P, g, per, x, ys, zs + 1, 2);
+            cd = (uint8_t)(1 + nn + 8 * nr);
+            fv = profile[x];
         } else if (ph == 1) {
             const int per = a.periodic;
             const int xm = x > 0 ? (P[((long long)(x - 1) * g.NY + ys) * g.NZ + zs] == 1) : 2;
@@ -169,11 +185,42 @@ int repack(const tf_geom& gg, const tf_operator& op, const float* padded, float*
     return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
 }
 
+// ElectrodeSolver's per-plane fluxes (taufactor/electrode.py:70-74) and field sums, one CTA per
+// (plane, volume): plane 0 (left_bc - c) / 0.5, plane x > 0 c[x-1] - c[x] (the float32 values of
+// -field[x] + field[x-1]), 0 where c or c[x-1] is 0; summed in float64 in a fixed order.
+__global__ void __launch_bounds__(256) k_layer_sums_electrode(const float* __restrict__ field, double* __restrict__ flux,
+                                                              double* __restrict__ csum, const Geo g, float glo) {
+    const int x = blockIdx.x, b = blockIdx.y;
+    const float left = 0.5f * glo;
+    const float* P = field + (long long)b * g.vol_f + (long long)x * g.plane_f;
+    double fs = 0.0, cs = 0.0;
+    const int rowlen = 2 * g.ZH;
+    for (long long it = threadIdx.x; it < (long long)g.NY * rowlen; it += blockDim.x) {
+        const int y = (int)(it / rowlen), pos = (int)(it - (long long)y * rowlen);
+        const int q = pos >= g.ZH ? 1 : 0, j = pos - q * g.ZH - HJ;
+        if (j < 0 || j >= half_len(g.NZ, q)) continue;
+        const long long o = (long long)(y + HY) * g.row_f + pos;
+        const float c = P[o];
+        const float cm = x > 0 ? P[o - g.plane_f] : glo;
+        float f = x > 0 ? __fsub_rn(cm, c) : __fdiv_rn(__fsub_rn(left, c), 0.5f);
+        if (c == 0.0f || cm == 0.0f) f = 0.0f;
+        fs += (double)f;
+        cs += (double)c;
+    }
+    block_sum_pair(fs, cs);
+    if (threadIdx.x == 0) {
+        flux[(long long)b * g.NX + x] = fs;
+        csum[(long long)b * g.NX + x] = cs;
+    }
+}
+
 int layer_sums(const tf_geom& gg, const tf_operator& op, const float* field, const uint8_t* code, double* flux,
                double* csum, cudaStream_t st) {
     const Geo g = make_geo(gg);
     dim3 grid(gg.nx, gg.batch);
-    if (op.kind == TF_KIND_MULTIPHASE)
+    if (op.kind == TF_KIND_ELECTRODE)
+        k_layer_sums_electrode<<<grid, 256, 0, st>>>(field, flux, csum, g, op.ghost_lo);
+    else if (op.kind == TF_KIND_MULTIPHASE)
         k_layer_sums<TF_KIND_MULTIPHASE><<<grid, 256, 0, st>>>(field, code, flux, csum, g, op);
     else if (op.kind == TF_KIND_ANISOTROPIC)
         k_layer_sums<TF_KIND_ANISOTROPIC><<<grid, 256, 0, st>>>(field, code, flux, csum, g, op);

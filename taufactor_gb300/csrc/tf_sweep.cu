@@ -26,6 +26,7 @@ __global__ void __launch_bounds__(256) k_plain(float* __restrict__ f, const uint
     __shared__ float4 tab[DIV_PAIRS * DIV_COPIES];
     if (KIND == TF_KIND_ANISOTROPIC)
         for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = op.divisor[i];
+    if (KIND == TF_KIND_ELECTRODE && threadIdx.x == 0) lut[0] = op.divisor[(blockIdx.z / a.g.NX) & 255];
     if (KIND == TF_KIND_MULTIPHASE)
         for (int i = threadIdx.x; i < 32 * 32; i += blockDim.x) lut[i] = op.face[i];
     if (KIND == TF_KIND_BINARY) fill_division_table(tab, threadIdx.x, blockDim.x);
@@ -155,6 +156,7 @@ int sweep_plain(const tf_geom& gg, const tf_operator& op, float* f, const uint8_
         case TF_KIND_BINARY: TF_PLAIN(TF_KIND_BINARY); break;
         case TF_KIND_ANISOTROPIC: TF_PLAIN(TF_KIND_ANISOTROPIC); break;
         case TF_KIND_MULTIPHASE: TF_PLAIN(TF_KIND_MULTIPHASE); break;
+        case TF_KIND_ELECTRODE: TF_PLAIN(TF_KIND_ELECTRODE); break;
         default: return TF_ERR_ARG;
     }
 #undef TF_PLAIN

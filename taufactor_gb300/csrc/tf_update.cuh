@@ -171,7 +171,25 @@ __device__ __forceinline__ float4 update4(float4 c, const float4& xp, const floa
     for (int i = 0; i < 4; ++i) {
         const float ci = comp(c, i);
         float sum, quot;
-        if (KIND == TF_KIND_ANISOTROPIC) {
+        if (KIND == TF_KIND_ELECTRODE) {
+            // the default neighbour sum (taufactor.py:95-103) over the divisor
+            // factor = nn + nr * k_0 in float32, inf where 0 (:47-55, electrode.py:46-62);
+            // lut[0] = k_0 of this volume, code = 1 + nn + 8 nr (0: not conductive)
+            sum = __fadd_rn(comp(xp, i), comp(xm, i));
+            sum = __fadd_rn(sum, comp(yp, i));
+            sum = __fadd_rn(sum, comp(ym, i));
+            sum = __fadd_rn(sum, comp(zp, i));
+            sum = __fadd_rn(sum, comp(zm, i));
+            if (RHS) sum = __fadd_rn(sum, comp(rv, i));
+            const uint32_t cd = byte_of(cc, i);
+            float div = __int_as_float(0x7f800000);
+            if (cd != 0u) {
+                const uint32_t m = cd - 1u;
+                const float d = __fadd_rn(static_cast<float>(m & 7u), __fmul_rn(static_cast<float>(m >> 3), lut[0]));
+                if (d != 0.0f) div = d;
+            }
+            quot = quotient(sum, div);
+        } else if (KIND == TF_KIND_ANISOTROPIC) {
             // taufactor.py:475-477: (x+1 + x-1) + Ky*(y+1 + y-1) + Kz*(z+1 + z-1)
             sum = __fadd_rn(comp(xp, i), comp(xm, i));
             sum = __fadd_rn(sum, __fmul_rn(ky, __fadd_rn(comp(yp, i), comp(ym, i))));

@@ -28,7 +28,7 @@ import numpy as np
 import torch
 
 from . import _capi, autotune
-from ._capi import (TF_KIND_ANISOTROPIC, TF_KIND_BINARY, TF_KIND_MULTIPHASE, TF_MAX_PHASES,
+from ._capi import (TF_KIND_ANISOTROPIC, TF_KIND_BINARY, TF_KIND_ELECTRODE, TF_KIND_MULTIPHASE, TF_MAX_PHASES,
                     TF_PERIODIC_Y, TF_PERIODIC_Z, TfGeom, TfOperator, check)
 from .percolation import spans_x
 
@@ -121,9 +121,7 @@ class SORSolver:
             self._fa = torch.empty(g.field_elems, dtype=torch.float32, device=dev)
             self._fb = torch.zeros(g.field_elems, dtype=torch.float32, device=dev)
             self._err = torch.zeros(1, dtype=torch.int32, device=dev)
-            sh = 1 / (2 * self.Nx)
-            # the reference's float32 linspace (taufactor.py:284-286), computed on the host
-            profile = torch.linspace(self.top_bc + sh, self.bot_bc - sh, self.Nx, dtype=torch.float32).to(dev)
+            profile = self._initial_profile().to(dev)
             phase_dev = torch.from_numpy(np.ascontiguousarray(phase, dtype=np.uint8)).to(dev)
             self._phase_dev, self._profile_dev = phase_dev, profile
             self._pack()
@@ -131,6 +129,12 @@ class SORSolver:
             self._csum_dev = torch.empty((self.batch_size, self.Nx), dtype=torch.float64, device=dev)
         self._cur, self._other = self._fa, self._fb
         self._field64 = None
+
+    def _initial_profile(self) -> torch.Tensor:
+        """float32 [Nx] initial value of a conductive voxel in plane x: the reference's float32
+        linspace (taufactor.py:284-286), computed on the host."""
+        sh = 1 / (2 * self.Nx)
+        return torch.linspace(self.top_bc + sh, self.bot_bc - sh, self.Nx, dtype=torch.float32)
 
     def _pack(self):
         with torch.cuda.device(self.device):
@@ -611,5 +615,161 @@ class MultiPhaseSolver(ThroughTransportSolver):
 
 class PeriodicMultiPhaseSolver(MultiPhaseSolver):
     """Multiphase, periodic in y and z (taufactor.py:623-656)."""
+
+    _periodic = TF_PERIODIC_Y | TF_PERIODIC_Z
+
+
+def compute_impedance_batched(R: np.ndarray, C: np.ndarray, freq: np.ndarray) -> np.ndarray:
+    """Impedance [B,F] of B transmission lines of Nx RC elements (taufactor/utils.py:75-98):
+    from the closed end, Z <- R_k + 1 / (i w C_k + 1 / Z), starting from Z = 1e50."""
+    if R.shape != C.shape:
+        raise ValueError(f"R and C must have same shape; got {R.shape} vs {C.shape}")
+    bs, nx = R.shape
+    if freq.ndim == 1:
+        w = freq[None, :].repeat(bs, axis=0)
+    elif freq.ndim == 2 and freq.shape[0] == bs:
+        w = freq
+    else:
+        raise ValueError("freq must be (F,) or (bs, F)")
+    Z = np.full_like(w, 1e50, dtype=complex)
+    for k in range(nx - 1, -1, -1):
+        Z = R[:, k][:, None] + 1.0 / (1j * w * C[:, k][:, None] + 1.0 / Z)
+    return Z
+
+
+class ElectrodeSolver(SORSolver):
+    """Electrode tortuosity (taufactor/electrode.py:13-125): concentration 1 at the inlet x = -1,
+    closed outlet, reaction to concentration 0 on every face between the conductive phase and
+    the reactive phase. tau = Re Z_sim / Re Z_ideal of the transmission line built from the
+    layer fluxes.
+
+    The sweep is the default neighbour sum over the divisor nn + nr * k_0 (nn conductive
+    neighbours with the inlet face counted twice, nr reactive neighbours, k_0 per volume as in
+    taufactor.py:47-55), computed on the device from the voxel's code.
+    """
+
+    _kind = TF_KIND_ELECTRODE
+
+    def __init__(self, img, conductive_label=1, reactive_label=0, omega=None, spacing=None, device="cuda"):
+        self.left_bc = 1.0
+        self.electrode_bc = 0.0
+        self.cond_label = conductive_label
+        self.reac_label = reactive_label
+        self.dx = spacing or 1
+        super().__init__(img, omega=omega, device=device)
+        self.vol_x = self._vol_x32
+        self.c_x = 0
+
+    def _phase_indices(self):
+        """uint8 1 = conductive, 2 = reactive; and the reference's float32 a_x, k_0, vol_x
+        (taufactor.py:40-55, electrode.py:36-62), from the same torch float32 operations."""
+        if self.batch_size > 256:
+            raise ValueError("ElectrodeSolver takes at most 256 volumes per batch")
+        cond = self.cpu_img == self.cond_label
+        reac = (self.cpu_img == self.reac_label) & ~cond
+        mask_t = torch.from_numpy(cond.astype(np.float32))
+        vol_x = torch.mean(mask_t, (2, 3))
+        r = torch.from_numpy(reac.astype(np.float32))
+        if self._periodic:
+            rp = torch.nn.functional.pad(r, (0, 0, 0, 0, 1, 1))  # x padded with 0, y/z wrap
+            reac_nn = torch.zeros_like(rp)
+            for dim in range(1, 4):
+                for dr in (1, -1):
+                    reac_nn += torch.roll(rp, dr, dim)
+            reac_nn = reac_nn[:, 1:-1]
+        else:
+            rp = torch.nn.functional.pad(r, (1, 1, 1, 1, 1, 1))
+            reac_nn = torch.zeros_like(rp)
+            for dim in range(1, 4):
+                for dr in (1, -1):
+                    reac_nn += torch.roll(rp, dr, dim)
+            reac_nn = reac_nn[:, 1:-1, 1:-1, 1:-1]
+        reac_nn[~torch.from_numpy(cond)] = 0.0
+        a_x = torch.sum(reac_nn, (2, 3)) / (self.Ny * self.Nz * self.dx)
+        k_0 = torch.mean(vol_x, 1) / torch.mean(a_x * self.dx, 1) / self.Nx ** 2
+        self.a_x = a_x.numpy()
+        self.k_0 = k_0.numpy()
+        self._vol_x32 = vol_x.numpy()
+        phase = np.where(cond, 1, np.where(reac, 2, 0)).astype(np.uint8)
+        return phase, cond
+
+    def _operator(self, omega):
+        op = TfOperator()
+        op.kind = self._kind
+        op.periodic = self._periodic
+        op.omega = float(F32(omega))
+        op.ghost_lo = 2 * self.left_bc  # the field's x padding (electrode.py:44)
+        op.ghost_hi = 0.0
+        op.ky = op.kz = 1.0
+        for i in range(256):
+            op.divisor[i] = float(self.k_0[i]) if i < len(self.k_0) else np.inf
+        return op
+
+    def _initial_profile(self) -> torch.Tensor:
+        """electrode.py:38-40: electrode_bc + (left_bc - electrode_bc) cosh(1 - x/Nx) / cosh(1) at
+        the voxel centres, in float64, then float32."""
+        x = np.arange(self.Nx) + 0.5
+        c_init = self.electrode_bc + (self.left_bc - self.electrode_bc) * np.cosh(1 - x / self.Nx) / np.cosh(1)
+        return torch.tensor(c_init, dtype=torch.float32)
+
+    def set_k_0(self, k_0):
+        """Use these float32 reaction prefactors (one per volume) instead of the ones computed
+        from the image. The reference takes k_0 as a float32 torch mean on its host, whose last
+        bit depends on the platform's reduction order; this pins a value (e.g. another machine's)."""
+        k = np.asarray(k_0, dtype=np.float32).reshape(-1)
+        if k.shape[0] != self.batch_size:
+            raise ValueError("one k_0 per volume")
+        self.k_0 = k
+        for b, v in enumerate(k):
+            self._op.divisor[b] = float(v)
+
+    def refine(self, *args, **kwargs):
+        raise NotImplementedError("FP64 refinement is built for the through-transport solvers only")
+
+    def _layer_sums_electrode(self):
+        with torch.cuda.device(self.device):
+            if self._flux_dev.shape[1] != self.Nx:
+                self._flux_dev = torch.empty((self.batch_size, self.Nx), dtype=torch.float64, device=self.device)
+            check(self._lib.tf_layer_sums(C.byref(self._geom), C.byref(self._op), _ptr(self._cur), _ptr(self._code),
+                                          _ptr(self._flux_dev), _ptr(self._csum_dev), self._stream()),
+                  "tf_layer_sums")
+            flux = self._flux_dev.cpu().numpy()
+            csum = self._csum_dev.cpu().numpy()
+            err = int(self._err.item())
+        if err:
+            self._err.zero_()
+            raise _capi.TfError(err, "tf_advance (device)")
+        area = float(self.Ny * self.Nz)
+        return flux / area, csum / area
+
+    def compute_metrics(self):
+        """electrode.py:64-103 on float64 layer means read back from the device."""
+        fluxes, c_raw = self._layer_sums_electrode()
+        vol_x = self.vol_x
+        c_x = np.divide(c_raw, vol_x, out=np.zeros(c_raw.shape), where=vol_x != 0)
+        relative_error = np.max(np.abs(c_x - self.c_x), axis=1)
+        self.c_x = c_x
+        fluxes_1d = np.concatenate((2 * (self.left_bc - c_x[:, :1]), (-c_x[:, 1:] + c_x[:, :-1])), axis=1)
+        fluxes_1d[:, 1:][vol_x[:, 1:] == 0] = 0
+        fluxes_1d[:, 1:][vol_x[:, :-1] == 0] = 0
+        eps = np.concatenate((vol_x[:, :1], 0.5 * (vol_x[:, :-1] + vol_x[:, 1:])), axis=1)
+        self.tau_x = np.divide(eps * fluxes_1d, fluxes, out=np.full_like(fluxes_1d, np.nan), where=fluxes != 0)
+        fluxes[:, :-1] -= fluxes[:, 1:]
+        self.k_x = np.divide(fluxes, c_x - self.electrode_bc, out=np.zeros_like(c_x),
+                             where=(c_x - self.electrode_bc) != 0) / self.k_0[:, None]
+        freq = np.mean(eps, axis=1, keepdims=True) / np.mean(self.a_x * self.dx, axis=1, keepdims=True) / self.Nx ** 2 * 2 ** -3
+        R = self.tau_x / eps
+        R[eps == 0] = 1e30
+        R[np.isnan(self.tau_x)] = 1e30
+        self.Z_sim = compute_impedance_batched(R, self.a_x * self.dx, freq)
+        R_ideal = 1 / np.mean(eps, axis=1)[:, None].repeat(self.Nx, axis=1)
+        C_ideal = np.mean(self.a_x * self.dx, axis=1)[:, None].repeat(self.Nx, axis=1)
+        self.Z_ideal = compute_impedance_batched(R_ideal, C_ideal, freq)
+        tau = self.Z_sim[:, 0].real / self.Z_ideal[:, 0].real
+        return tau, relative_error
+
+
+class PeriodicElectrodeSolver(ElectrodeSolver):
+    """Electrode solver, periodic in y and z (electrode.py:128-157)."""
 
     _periodic = TF_PERIODIC_Y | TF_PERIODIC_Z

@@ -82,6 +82,15 @@ def random_labels(shape, seed, n=3):
     return np.random.default_rng(seed).integers(0, n, shape).astype(np.uint8)
 
 
+def _blur_labels(shape, seed):
+    """Three labels from the argmax of three blurred noise fields (sigma 1.5)."""
+    from scipy.ndimage import gaussian_filter
+
+    rng = np.random.default_rng(seed)
+    f = np.stack([gaussian_filter(rng.standard_normal(shape), 1.5) for _ in range(3)])
+    return np.argmax(f, axis=0).astype(np.uint8)
+
+
 # name -> (kind, input builder, constructor kwargs, solve kwargs, reference test it restates)
 SOLVE_CASES = {
     "blocks_cube": ("binary", lambda: _blocks((20, 20, 20)), {}, {}, "test_taufactor.py:12-19"),
@@ -118,6 +127,16 @@ SOLVE_CASES = {
     "bernoulli100": ("binary", bernoulli_100, {}, {"conv_crit": 2e-2}, "100^3 Bernoulli(0.5), seed 0"),
     "bernoulli100_periodic": ("periodic", bernoulli_100, {}, {"conv_crit": 2e-2},
                               "100^3 Bernoulli(0.5), seed 0, periodic y/z"),
+    # the reference has no test of its electrode solvers (taufactor/electrode.py:13-157); these
+    # cases are its own outputs on seeded label volumes (1 = conductive, 0 = reactive, 2 = inert)
+    "el_labels": ("electrode", lambda: random_labels((20, 12, 14), 5), {}, {"conv_crit": 1e-3},
+                  "electrode.py:13-125"),
+    "el_batch": ("electrode", lambda: random_labels((2, 11, 9, 13), 7), {}, {"conv_crit": 1e-3},
+                 "electrode.py:13-125"),
+    "el_blur": ("electrode", lambda: _blur_labels((24, 16, 16), 8), {}, {"conv_crit": 1e-3},
+                "electrode.py:13-125"),
+    "pel_batch": ("periodic_electrode", lambda: random_labels((2, 16, 10, 12), 6), {}, {"conv_crit": 1e-3},
+                  "electrode.py:128-157"),
 }
 
 # name -> (kind, input builder, constructor kwargs, number of half-sweeps)
@@ -131,4 +150,6 @@ SWEEP_CASES = {
                       {"diffusivities": {0: 0.0, 1: 1.0, 2: 0.1}}, 57),
     "sw_periodic_multiphase": ("periodic_multiphase", lambda: random_labels((10, 9, 11), 17),
                                {"diffusivities": {0: 0.3, 1: 1.0, 2: 0.1}}, 57),
+    "sw_electrode": ("electrode", lambda: random_labels((2, 13, 10, 12), 18), {}, 57),
+    "sw_periodic_electrode": ("periodic_electrode", lambda: random_labels((12, 10, 14), 19), {}, 57),
 }

@@ -32,6 +32,8 @@ CLASS_OF = {
     "anisotropic": "AnisotropicSolver",
     "multiphase": "MultiPhaseSolver",
     "periodic_multiphase": "PeriodicMultiPhaseSolver",
+    "electrode": "ElectrodeSolver",
+    "periodic_electrode": "PeriodicElectrodeSolver",
 }
 
 
@@ -59,13 +61,18 @@ def main():
             s = build(tau, kind, img, kw)
             s.solve(verbose=False, **solve_kw)
         out[f"{name}/tau"] = np.asarray(s.tau, dtype=np.float64)
-        out[f"{name}/D_eff"] = np.asarray(s.D_eff, dtype=np.float64)
         out[f"{name}/iter"] = np.asarray(s.iter)
         out[f"{name}/converged"] = np.asarray(bool(s.converged))
-        out[f"{name}/flux_1d"] = np.asarray(s.flux_1d, dtype=np.float64)
         out[f"{name}/c_x"] = np.asarray(s.c_x, dtype=np.float64)
         out[f"{name}/tau_x"] = np.asarray(s.tau_x, dtype=np.float64)
-        print(f"{name:24s} iter={s.iter:5d} tau={np.asarray(s.tau)} D_eff={np.asarray(s.D_eff)}")
+        if kind in ("electrode", "periodic_electrode"):
+            out[f"{name}/k_x"] = np.asarray(s.k_x, dtype=np.float64)
+            out[f"{name}/k_0"] = np.asarray(s.k_0, dtype=np.float32)
+            out[f"{name}/a_x"] = np.asarray(s.a_x, dtype=np.float32)
+        else:
+            out[f"{name}/D_eff"] = np.asarray(s.D_eff, dtype=np.float64)
+            out[f"{name}/flux_1d"] = np.asarray(s.flux_1d, dtype=np.float64)
+        print(f"{name:24s} iter={s.iter:5d} tau={np.asarray(s.tau)}")
     for name, (kind, make, kw, n) in SWEEP_CASES.items():
         img = make()
         s = build(tau, kind, img, kw)
@@ -79,6 +86,8 @@ def main():
                 s.field[:, 1:-1, 1:-1, 1:-1] += inc
                 s.iter += 1
         out[f"{name}/field"] = s.field.numpy().copy()
+        if kind in ("electrode", "periodic_electrode"):
+            out[f"{name}/k_0"] = np.asarray(s.k_0, dtype=np.float32)
         print(f"{name:24s} field {tuple(s.field.shape)} after {n} half-sweeps")
     np.savez_compressed(os.path.join(HERE, "reference_outputs.npz"), **out)
 

@@ -32,11 +32,17 @@ def test_oracle_solve_matches_reference(name, golden):
     assert o.iter == int(golden[f"{name}/iter"])
     assert bool(o.converged) == bool(golden[f"{name}/converged"])
     tau_ref = golden[f"{name}/tau"]
-    d_ref = golden[f"{name}/D_eff"]
     assert np.array_equal(np.isinf(o.tau), np.isinf(tau_ref))
     fin = np.isfinite(tau_ref)
     # the oracle reduces layer means in float64, the reference in float32
     np.testing.assert_allclose(o.tau[fin], tau_ref[fin], rtol=2e-6)
+    if o.electrode:
+        np.testing.assert_array_equal(o.k_0, golden[f"{name}/k_0"])
+        np.testing.assert_array_equal(o.a_x, golden[f"{name}/a_x"])
+        np.testing.assert_allclose(o.c_x, golden[f"{name}/c_x"], rtol=1e-5, atol=1e-7)
+        np.testing.assert_allclose(o.k_x, golden[f"{name}/k_x"], rtol=1e-3, atol=1e-3)
+        return
+    d_ref = golden[f"{name}/D_eff"]
     np.testing.assert_allclose(o.D_eff, d_ref, rtol=2e-6, atol=1e-9)
     np.testing.assert_allclose(o.flux_1d, golden[f"{name}/flux_1d"], rtol=1e-4, atol=1e-7)
 

@@ -21,6 +21,8 @@ CLASSES = {
     "anisotropic": tg.AnisotropicSolver,
     "multiphase": tg.MultiPhaseSolver,
     "periodic_multiphase": tg.PeriodicMultiPhaseSolver,
+    "electrode": tg.ElectrodeSolver,
+    "periodic_electrode": tg.PeriodicElectrodeSolver,
 }
 
 
@@ -44,20 +46,26 @@ def interior_and_x_ghosts(f):
 def test_half_sweeps_bitwise_vs_reference(name, golden):
     kind, make, kw, n = SWEEP_CASES[name]
     s = make_solver(kind, make(), kw)
+    if kind in ("electrode", "periodic_electrode"):
+        # the reference's k_0 is a float32 torch mean whose last bit depends on the host
+        k_ref = golden[f"{name}/k_0"]
+        np.testing.assert_allclose(s.k_0, k_ref, rtol=2.0 ** -22, atol=0)
+        s.set_k_0(k_ref)
     s._advance(n)
     got = s.field.cpu().numpy()
     ref = golden[f"{name}/field"]
     assert np.array_equal(interior_and_x_ghosts(got), interior_and_x_ghosts(ref))
 
 
-@pytest.mark.parametrize("kind", ["binary", "periodic", "anisotropic", "multiphase", "periodic_multiphase"])
+@pytest.mark.parametrize("kind", ["binary", "periodic", "anisotropic", "multiphase", "periodic_multiphase",
+                                  "electrode", "periodic_electrode"])
 @pytest.mark.parametrize("shape", [(1, 23, 40, 70), (2, 9, 17, 33), (1, 5, 64, 128), (1, 30, 8, 16),
                                    (1, 100, 24, 40)])
 def test_chunked_half_sweeps_bitwise_vs_oracle(kind, shape):
     """Every chunk length 1..9 (several tiled launches, odd/even colour starts) matches. The
     long-x shape runs each tile column as several x-chunks (few columns for 152 SMs)."""
     seed = sum(shape)
-    if kind in ("multiphase", "periodic_multiphase"):
+    if kind in ("multiphase", "periodic_multiphase", "electrode", "periodic_electrode"):
         img = random_labels(shape, seed)
         kw = {"diffusivities": {0: 0.0, 1: 1.0, 2: 0.1}}
     else:
@@ -75,6 +83,9 @@ def test_chunked_half_sweeps_bitwise_vs_oracle(kind, shape):
 def test_solve_matches_reference(name, golden):
     kind, make, kw, solve_kw, _ = SOLVE_CASES[name]
     s = make_solver(kind, make(), kw)
+    if kind in ("electrode", "periodic_electrode"):
+        np.testing.assert_allclose(s.k_0, golden[f"{name}/k_0"], rtol=2.0 ** -22, atol=0)
+        s.set_k_0(golden[f"{name}/k_0"])
     ret = s.solve(verbose=False, **solve_kw)
     assert s.iter == int(golden[f"{name}/iter"])
     assert bool(s.converged) == bool(golden[f"{name}/converged"])
@@ -82,9 +93,13 @@ def test_solve_matches_reference(name, golden):
     assert np.array_equal(np.isinf(s.tau), np.isinf(tau_ref))
     fin = np.isfinite(tau_ref)
     np.testing.assert_allclose(s.tau[fin], tau_ref[fin], rtol=2e-6)
+    assert ret.shape == golden[f"{name}/tau_x"].shape
+    if kind in ("electrode", "periodic_electrode"):
+        np.testing.assert_allclose(s.c_x, golden[f"{name}/c_x"], rtol=1e-5, atol=1e-7)
+        np.testing.assert_allclose(s.k_x, golden[f"{name}/k_x"], rtol=1e-3, atol=1e-3)
+        return
     np.testing.assert_allclose(s.D_eff, golden[f"{name}/D_eff"], rtol=2e-6, atol=1e-9)
     np.testing.assert_allclose(s.flux_1d, golden[f"{name}/flux_1d"], rtol=1e-4, atol=1e-7)
-    assert ret.shape == golden[f"{name}/tau_x"].shape
 
 
 def test_reference_known_answers():
