@@ -440,6 +440,41 @@ def design_loop(dev, side=768, steps=50, lr=0.05, lam=0.5, tol=1e-8, conv_crit=1
             "direction_fd_rel_err": abs(fd - ad) / abs(fd), "fd_h": h, "per_step": rows}
 
 
+def electrode_throughput(dev, batch=4, side=256, conv_crit=1e-3, cpu_half_sweeps=10):
+    """ElectrodeSolver on batch x side^3 three-label volumes (argmax of three blurred noise fields,
+    sigma 2, default_rng(4000 + i); 1 = pore (conductive), 0 = active material (reactive),
+    2 = inert): one solve to the reference's rule, voxel-updates/s of the whole solve, the
+    fused kernel's effective bandwidth, and the oracle port's sweeps on the host cores."""
+    import torch
+    from scipy.ndimage import gaussian_filter
+
+    import taufactor_gb300 as tg
+    from oracle.sor import OracleSolve
+
+    rngs = [np.random.default_rng(4000 + i) for i in range(batch)]
+    vols = np.stack([np.argmax(np.stack([gaussian_filter(r.standard_normal((side,) * 3, dtype=np.float32), 2.0)
+                                         for _ in range(3)]), axis=0).astype(np.uint8) for r in rngs])
+    s = tg.ElectrodeSolver(vols, device=dev)
+    s.solve(verbose=False, conv_crit=conv_crit, iter_limit=200)  # warm-up
+    s = tg.ElectrodeSolver(vols, device=dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    s.solve(verbose=False, conv_crit=conv_crit)
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    vu = s.iter * vols.size / 2
+    o = OracleSolve(vols[:1, : side // 4], kind="electrode")  # a quarter of one volume on the host
+    t1 = time.perf_counter()
+    o.half_sweep(cpu_half_sweeps)
+    tc = time.perf_counter() - t1
+    return {"workload": f"ElectrodeSolver {batch}x{side}^3, labels argmax of 3 blurred fields sigma 2 (rng 4000+i)",
+            "conv_crit": conv_crit, "half_sweeps": int(s.iter), "converged": bool(s.converged),
+            "tau": [float(v) for v in s.tau], "solve_s": t, "voxel_updates_per_s": vu / t,
+            "effective_GBps_8B_per_update": vu / t * 8 / 1e9,
+            "cpu_oracle_voxel_updates_per_s": cpu_half_sweeps * o.factor.size / 2 / tc,
+            "cpu_sample": f"oracle port, 1 process, {cpu_half_sweeps} half-sweeps on 1x{side // 4}x{side}x{side}"}
+
+
 def adjoint_cost(dev, side=320, fd_voxels=0, tol=1e-12, fd_tol=1e-14):
     """Per-voxel conductivity kappa = sigmoid(blur_2(2 N(0,1))) on side^3 (default_rng(3003)):
     forward solve + FP64 refinement, then the adjoint gradient; times and, with fd_voxels > 0,
@@ -571,7 +606,7 @@ def main():
     ap.add_argument("--side", type=int, default=256, help="--profile: volume side")
     ap.add_argument("--half-sweeps", type=int, default=40, help="--profile: half-sweeps")
     ap.add_argument("--periodic", action="store_true", help="--profile: PeriodicSolver")
-    ap.add_argument("--workload", choices=["uneven", "adjoint", "design"], default=None,
+    ap.add_argument("--workload", choices=["uneven", "adjoint", "design", "electrode"], default=None,
                     help="print the secondary measurement of this workload only")
     ap.add_argument("--fd-voxels", type=int, default=0, help="--workload adjoint: finite-difference check")
     ap.add_argument("--adj-side", dest="adj_side", type=int, default=320, help="--workload adjoint: volume side")
@@ -584,6 +619,8 @@ def main():
         dev = torch.device("cuda", 0)
         if args.workload == "uneven":
             print(json.dumps(uneven_batch(dev)), flush=True)
+        elif args.workload == "electrode":
+            print(json.dumps(electrode_throughput(dev)), flush=True)
         elif args.workload == "design":
             print(json.dumps(design_loop(dev, args.design_side, args.design_steps)), flush=True)
         else:
