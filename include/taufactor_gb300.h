@@ -283,6 +283,16 @@ int tf_kappa_pack(const tf_geom* g, const tf_operator* op, const float* kappa_de
 int tf_kappa_advance(const tf_geom* g, const tf_operator* op, float* field_dev, const float* kappa_split_dev,
                      const float* rhs_dev, int first_colour, int n_half, void* stream);
 
+/* Spanning-path test of the zero-flux branch of the convergence check (taufactor.py:318-327,
+ * extract_through_feature(mask, 1, 'x'), taufactor/metrics/connectivity.py:138-213): for every
+ * volume, whether a face-connected cluster of conductive voxels (conductive[phase] != 0, host
+ * table of 256 entries; no periodic wrap) touches both x = 0 and x = nx - 1.
+ *   phase_dev  uint8 [batch][nx][ny][nz]; labels_dev int32 scratch of the same size
+ *   spans_dev  int32 [batch]: 1 / 0.  err_dev: TF_ERR_TIMEOUT if a bounded loop ran out.
+ * batch * nx * ny * nz must stay below 2^31. */
+int tf_spans_x(int batch, int nx, int ny, int nz, const uint8_t* phase_dev, const uint8_t* conductive,
+               int32_t* labels_dev, int32_t* spans_dev, int32_t* err_dev, void* stream);
+
 /* The operator's faces for tf_kappa_advance_faces, computed once per kappa field (float32, the
  * values the sweeps use; taufactor.py:586-603 with a per-voxel diffusivity): fx_dev holds
  * batch * (nx + 1) planes of field_elems / (batch * nx) floats each (plane x + 1 = the face

@@ -26,7 +26,7 @@ EXPORTS = (
     "tf_batch_describe_rhs", "tf_batch_advance_rhs",
     "tf_batch_converge_static", "tf_kappa_pack", "tf_kappa_advance", "tf_kappa_layer_sums",
     "tf_kappa_residual_f64", "tf_kappa_adjoint_rhs", "tf_kappa_gradient", "tf_split_to_natural_f64",
-    "tf_kappa_faces", "tf_kappa_advance_faces",
+    "tf_kappa_faces", "tf_kappa_advance_faces", "tf_spans_x",
 )
 TF_BATCH_ACTIVE, TF_BATCH_CONVERGED, TF_BATCH_NEEDS_HOST = 0, 1, 2
 
@@ -108,6 +108,7 @@ def load():
         "tf_kappa_pack": (i32, [G, O, vp, vp, vp, vp, vp]),
         "tf_kappa_advance": (i32, [G, O, vp, vp, vp, i32, i32, vp]),
         "tf_kappa_faces": (i32, [G, vp, vp, vp, vp, vp, vp]),
+        "tf_spans_x": (i32, [i32, i32, i32, i32, vp, vp, vp, vp, vp, vp]),
         "tf_kappa_advance_faces": (i32, [G, O, vp, vp, vp, vp, vp, vp, i32, i32, vp]),
         "tf_kappa_layer_sums": (i32, [G, vp, i32, i32, vp, vp, vp, vp]),
         "tf_kappa_residual_f64": (i32, [G, O, vp, vp, vp, i32, vp, vp, vp, vp]),

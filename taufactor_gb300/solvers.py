@@ -155,6 +155,32 @@ class SORSolver:
     def _stream(self):
         return torch.cuda.current_stream(self.device).cuda_stream
 
+    def _conductive_table(self):
+        t = (C.c_uint8 * 256)()
+        if self._kind == TF_KIND_MULTIPHASE:
+            for i in range(32):
+                t[i] = self._op.conductive[i]
+        else:
+            t[1] = 1
+        return t
+
+    def spans_x_device(self) -> np.ndarray:
+        """Whether each volume has a face-connected conductive path from x = 0 to x = Nx-1
+        (bool [B]), by the device's union-find labelling (tf_spans_x); the reference labels on
+        the host (taufactor.py:318-327, metrics/connectivity.py:138-213)."""
+        with torch.cuda.device(self.device):
+            labels = torch.empty(self.batch_size * self.Nx * self.Ny * self.Nz, dtype=torch.int32, device=self.device)
+            spans = torch.empty(self.batch_size, dtype=torch.int32, device=self.device)
+            check(self._lib.tf_spans_x(self.batch_size, self.Nx, self.Ny, self.Nz, _ptr(self._phase_dev),
+                                       self._conductive_table(), _ptr(labels), _ptr(spans), _ptr(self._err),
+                                       self._stream()), "tf_spans_x")
+            out = spans.cpu().numpy() != 0
+            err = int(self._err.item())
+        if err:
+            self._err.zero_()
+            raise _capi.TfError(err, "tf_spans_x (device)")
+        return out
+
     def tune(self, half_sweeps: int = 48) -> dict:
         """Pick the fastest tile shape / half-sweeps per launch for these volumes (results unchanged)."""
         return autotune.tune(self, half_sweeps)
@@ -412,9 +438,16 @@ def layer_metrics(s, flux_1d: np.ndarray, c_x_raw: np.ndarray):
     flux_from_c[s.vol_x[:, :-1] == 0] = 0
     eps = 0.5 * (s.vol_x[:, :-1] + s.vol_x[:, 1:])
     s.tau_x = np.divide(eps * flux_from_c, flux_1d, out=np.full_like(flux_from_c, np.nan), where=flux_1d != 0)
+    spans = None
     for b in range(s.batch_size):
         if (fl_min[b] == 0) or (fl_max[b] == 0) or (mean_fl[b] == 0):
-            if not spans_x(np.isin(s.cpu_img[b], s.conductive_labels)):
+            if hasattr(s, "spans_x_device"):  # the solver's phases are on the device
+                if spans is None:
+                    spans = s.spans_x_device()
+                percolates = bool(spans[b])
+            else:
+                percolates = spans_x(np.isin(s.cpu_img[b], s.conductive_labels))
+            if not percolates:
                 print(f"Warning: batch element {b} has no percolating path!")
                 relative_error[b] = 0
                 D_rel[b] = 0

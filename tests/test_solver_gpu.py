@@ -211,3 +211,36 @@ def test_tile_variants_bitwise(kind, tile, k_max, shape):
         s._advance(n)
         o.half_sweep(n)
         assert np.array_equal(interior_and_x_ghosts(s.field.cpu().numpy()), interior_and_x_ghosts(o.field)), n
+
+
+@pytest.mark.parametrize("p", [0.25, 0.31, 0.4])
+def test_device_spanning_test_matches_host_labelling(p):
+    """tf_spans_x (union-find on the device) agrees with the host's face-connected labelling on
+    random masks near the site-percolation threshold, in batches of uneven outcome."""
+    from taufactor_gb300.percolation import spans_x
+
+    for seed, shape in enumerate([(6, 21, 17, 19), (3, 40, 9, 33), (2, 9, 64, 48)]):
+        img = (np.random.default_rng(1000 * seed + int(100 * p)).random(shape) < p).astype(np.uint8)
+        s = tg.Solver(img)
+        got = s.spans_x_device()
+        want = np.array([spans_x(img[b] == 1) for b in range(shape[0])])
+        assert np.array_equal(got, want), (shape, got, want)
+
+
+def test_device_spanning_test_long_path():
+    """A single serpentine path through every row (long union-find chains) and its cut copy."""
+    from taufactor_gb300.percolation import spans_x
+
+    img = np.zeros((64, 66, 33), dtype=np.uint8)
+    for x in range(64):
+        img[x, x, :] = 1  # one row per plane, joined to the next plane's row at alternating ends
+        if x + 1 < 64:
+            img[x + 1, x, 32 if x % 2 else 0] = 1
+    assert spans_x(img == 1)
+    cut = img.copy()
+    cut[40] = 0
+    for v in (img, cut):
+        s = tg.Solver(v)
+        assert bool(s.spans_x_device()[0]) == spans_x(v == 1)
+    mp = tg.MultiPhaseSolver(np.where(img == 1, 2, 0).astype(np.uint8), {0: 0.0, 2: 0.7})
+    assert bool(mp.spans_x_device()[0])
