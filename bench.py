@@ -475,6 +475,101 @@ def electrode_throughput(dev, batch=4, side=256, conv_crit=1e-3, cpu_half_sweeps
             "cpu_sample": f"oracle port, 1 process, {cpu_half_sweeps} half-sweeps on 1x{side // 4}x{side}x{side}"}
 
 
+def impedance_volume(side, seed, porosity=0.45, sigma=2.0):
+    """Pore (1) / active material (0) from a blurred noise field thresholded at its `porosity`
+    quantile; pore clusters that do not reach the inlet plane x = 0 become inert (2)."""
+    from scipy.ndimage import gaussian_filter, label
+
+    f = gaussian_filter(np.random.default_rng(seed).standard_normal((side,) * 3, dtype=np.float32), sigma)
+    vol = (f > np.quantile(f, 1 - porosity)).astype(np.uint8)
+    lab, _ = label(vol)
+    keep = np.unique(lab[0][lab[0] > 0])
+    vol[(vol == 1) & ~np.isin(lab, keep)] = 2
+    return vol
+
+
+def impedance_throughput(dev, side=256, nyq_side=64, cpu_half_sweeps=4):
+    """ImpedanceSolver (complex128) on a side^3 pore volume (impedance_volume, seed 5000): the
+    drop-in tau_e solve (two frequencies in sequence, the reference's rule), the sweep kernel
+    alone timed with CUDA events (22 double operations per voxel-update), the oracle's
+    half-sweeps on a quarter of the volume on the host; and the 26-frequency Nyquist sweep of a
+    nyq_side^3 volume, sequential (the reference's loop) against solve_frequencies."""
+    import contextlib
+    import io
+
+    import torch
+
+    import taufactor_gb300 as tg
+    from oracle import impedance as oi
+
+    vol = impedance_volume(side, 5000)
+    quiet = contextlib.redirect_stdout(io.StringIO())
+    with quiet:
+        w = tg.ImpedanceSolver(vol, device=dev)
+        w.solve(verbose=False, iter_limit=200)  # warm-up
+    s = tg.ImpedanceSolver(vol, device=dev)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    with contextlib.redirect_stdout(io.StringIO()):
+        s.solve(verbose=False)
+    torch.cuda.synchronize()
+    t = time.perf_counter() - t0
+    vu = s.sum_iter * vol.size / 2
+    # kernel only: 200 half-sweeps of the converged field
+    st = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    n = 200
+    s.iter = 0
+    e0.record(st)
+    s._advance(n)
+    e1.record(st)
+    torch.cuda.synchronize()
+    k_ms = e0.elapsed_time(e1) / n
+    k_rate = vol.size / 2 / (k_ms * 1e-3)
+    # host: the oracle's numpy half-sweep on a quarter of the volume
+    stq = oi.setup(vol[: side // 4])
+    fq = oi.init_field(stq, float(stq["frequency"][0]))
+    code = (stq["nn"] + 8 * stq["nr"]).astype(np.int64)
+    code[stq["mask"] == 0] = 0
+    fac = oi.factor_table(float(stq["frequency"][0]))[code]
+    cb = oi.chequerboard(stq["shape"], s.omega)
+    t1 = time.perf_counter()
+    for i in range(cpu_half_sweeps):
+        oi.half_sweep(fq, fac, cb[i % 2], False)
+    tc = time.perf_counter() - t1
+    # Nyquist: 26 frequencies in sequence (reference loop) and side by side
+    nv = impedance_volume(nyq_side, 5001)
+    with contextlib.redirect_stdout(io.StringIO()):
+        a = tg.ImpedanceSolver(nv, device=dev, mode="nyquist")
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        a.solve(verbose=False)
+        torch.cuda.synchronize()
+        t_seq = time.perf_counter() - t2
+    b = tg.ImpedanceSolver(nv, device=dev, mode="nyquist")
+    torch.cuda.synchronize()
+    t3 = time.perf_counter()
+    r = b.solve_frequencies()
+    torch.cuda.synchronize()
+    t_bat = time.perf_counter() - t3
+    ok = np.isfinite(r["impedance"]) & np.array([np.isfinite(z) for z in a.impedance])
+    agree = [abs(complex(a.impedance[k]) - r["impedance"][k]) / abs(r["impedance"][k])
+             for k in np.flatnonzero(ok) if a.converged_freq[k] and r["converged"][k]]
+    return {"workload": f"ImpedanceSolver {side}^3 pore volume (porosity 0.45, sigma 2, rng 5000; isolated pores inert)",
+            "dtype": "complex128", "half_sweeps": int(s.sum_iter), "converged_freq": s.converged_freq,
+            "taus": [float(np.asarray(v)[0]) for v in s.taus], "solve_s": t, "voxel_updates_per_s": vu / t,
+            "kernel_ms_per_half_sweep": k_ms, "kernel_voxel_updates_per_s": k_rate,
+            "kernel_fp64_Gops": 22 * k_rate / 1e9,
+            "cpu_oracle_voxel_updates_per_s": cpu_half_sweeps * vol[: side // 4].size / 2 / tc,
+            "cpu_sample": f"oracle port (numpy), 1 process, {cpu_half_sweeps} half-sweeps on {side // 4}x{side}x{side}",
+            "nyquist": {"volume": f"{nyq_side}^3 (rng 5001)", "frequencies": int(len(a.frequency)),
+                        "sequential_s": t_seq, "sequential_half_sweeps": int(a.sum_iter),
+                        "sequential_converged": int(sum(a.converged_freq)),
+                        "side_by_side_s": t_bat, "side_by_side_half_sweeps": [int(v) for v in r["iters"]],
+                        "side_by_side_converged": int(r["converged"].sum()),
+                        "max_rel_diff_converged": float(max(agree)) if agree else None}}
+
+
 def adjoint_cost(dev, side=320, fd_voxels=0, tol=1e-12, fd_tol=1e-14):
     """Per-voxel conductivity kappa = sigmoid(blur_2(2 N(0,1))) on side^3 (default_rng(3003)):
     forward solve + FP64 refinement, then the adjoint gradient; times and, with fd_voxels > 0,
@@ -606,7 +701,7 @@ def main():
     ap.add_argument("--side", type=int, default=256, help="--profile: volume side")
     ap.add_argument("--half-sweeps", type=int, default=40, help="--profile: half-sweeps")
     ap.add_argument("--periodic", action="store_true", help="--profile: PeriodicSolver")
-    ap.add_argument("--workload", choices=["uneven", "adjoint", "design", "electrode"], default=None,
+    ap.add_argument("--workload", choices=["uneven", "adjoint", "design", "electrode", "impedance"], default=None,
                     help="print the secondary measurement of this workload only")
     ap.add_argument("--fd-voxels", type=int, default=0, help="--workload adjoint: finite-difference check")
     ap.add_argument("--adj-side", dest="adj_side", type=int, default=320, help="--workload adjoint: volume side")
@@ -621,6 +716,8 @@ def main():
             print(json.dumps(uneven_batch(dev)), flush=True)
         elif args.workload == "electrode":
             print(json.dumps(electrode_throughput(dev)), flush=True)
+        elif args.workload == "impedance":
+            print(json.dumps(impedance_throughput(dev)), flush=True)
         elif args.workload == "design":
             print(json.dumps(design_loop(dev, args.design_side, args.design_steps)), flush=True)
         else:

@@ -339,6 +339,43 @@ int tf_kappa_gradient(const tf_geom* g, const tf_operator* op, const double* fie
 /* double field layout -> natural [batch][nx][ny][nz]. */
 int tf_split_to_natural_f64(const tf_geom* g, const double* split_dev, double* natural_dev, void* stream);
 
+/* ---- Impedance (tau_e) solve: ImpedanceSolver / PeriodicImpedanceSolver ----------------------
+ * (taufactor/electrode.py:160-402). One volume; n_freq frequencies solved side by side. The field
+ * is complex128 in the reference's padded layout [n_freq][nx+2][ny+2][nz+2], interleaved
+ * (re, im) doubles, 16-byte aligned. A voxel's code is 0 outside the conductive phase, else
+ * 0x80 | (nn + 8 nr) with nn its conductive face neighbours (the inlet ghost x = -1 counted 2)
+ * and nr its reactive ones; the factor table holds 1 / (nn + i frc nr) per frequency at index
+ * nn + 8 nr (entry 0 = 0), TF_IMP_TABLE complex entries per frequency. */
+#define TF_IMP_TABLE 56
+
+/* Codes and per-plane counts (conductive voxels, reactive faces) as uint64 [nx][2] from phase
+ * bits (bit 0 conductive, bit 1 reactive) of uint8 [nx][ny][nz]; periodic in y and z if set.
+ * Replaces ImpedanceSolver.count_neighbours (electrode.py:235-264), the periodic variant
+ * (:373-396) and the vol_x / a_x sums of __init__ (:186-187). */
+int tf_impedance_pack(int nx, int ny, int nz, int periodic, const uint8_t* phase_dev, uint8_t* code_dev,
+                      uint64_t* plane_counts_dev, void* stream);
+
+/* Initial field: phi[f][x] (complex, [n_freq][nx] interleaved) on conductive voxels, 0 elsewhere,
+ * ghost_lo on the inlet ghost plane's interior, 0 on every other ghost. Replaces
+ * ImpedanceSolver.init_field_internal (electrode.py:214-233), phi computed by the caller. */
+int tf_impedance_fill(int n_freq, int nx, int ny, int nz, const uint8_t* code_dev, const double* phi_dev,
+                      double ghost_lo, double* field_dev, void* stream);
+
+/* n_half half-sweeps; half-sweep s updates colour (first_iter + s) % 2 of every frequency whose
+ * active_dev byte is non-zero (active_dev NULL: all), after the periodic ghost copy if periodic.
+ * Replaces the loop body of ImpedanceSolver.solve (electrode.py:302-309) with
+ * PeriodicImpedanceSolver.apply_boundary_conditions (:398-402). */
+int tf_impedance_sweep(int n_freq, int nx, int ny, int nz, int periodic, double* field_dev,
+                       const uint8_t* code_dev, const double* table_dev, const uint8_t* active_dev,
+                       double omega, int first_iter, int n_half, void* stream);
+
+/* Per-plane sums of |c| (double [n_freq][nx]), sums of the inlet flux 2 left_bc - 2 c over plane
+ * 0 where c != 0 (double [n_freq][2]: re, im) and the NaN cells per frequency (int32 [n_freq]).
+ * Replaces the reductions of ImpedanceSolver.compute_metrics (electrode.py:379-392),
+ * calc_input_impedance (:324-330) and the NaN test of solve (:293). */
+int tf_impedance_metrics(int n_freq, int nx, int ny, int nz, const double* field_dev, double left_bc,
+                         double* abs_sum_dev, double* influx_sum_dev, int32_t* nan_count_dev, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

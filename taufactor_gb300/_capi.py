@@ -27,7 +27,9 @@ EXPORTS = (
     "tf_batch_converge_static", "tf_kappa_pack", "tf_kappa_advance", "tf_kappa_layer_sums",
     "tf_kappa_residual_f64", "tf_kappa_adjoint_rhs", "tf_kappa_gradient", "tf_split_to_natural_f64",
     "tf_kappa_faces", "tf_kappa_advance_faces", "tf_spans_x",
+    "tf_impedance_pack", "tf_impedance_fill", "tf_impedance_sweep", "tf_impedance_metrics",
 )
+TF_IMP_TABLE = 56
 TF_BATCH_ACTIVE, TF_BATCH_CONVERGED, TF_BATCH_NEEDS_HOST = 0, 1, 2
 
 
@@ -109,6 +111,10 @@ def load():
         "tf_kappa_advance": (i32, [G, O, vp, vp, vp, i32, i32, vp]),
         "tf_kappa_faces": (i32, [G, vp, vp, vp, vp, vp, vp]),
         "tf_spans_x": (i32, [i32, i32, i32, i32, vp, vp, vp, vp, vp, vp]),
+        "tf_impedance_pack": (i32, [i32, i32, i32, i32, vp, vp, vp, vp]),
+        "tf_impedance_fill": (i32, [i32, i32, i32, i32, vp, vp, C.c_double, vp, vp]),
+        "tf_impedance_sweep": (i32, [i32, i32, i32, i32, i32, vp, vp, vp, vp, C.c_double, i32, i32, vp]),
+        "tf_impedance_metrics": (i32, [i32, i32, i32, i32, vp, C.c_double, vp, vp, vp, vp]),
         "tf_kappa_advance_faces": (i32, [G, O, vp, vp, vp, vp, vp, vp, i32, i32, vp]),
         "tf_kappa_layer_sums": (i32, [G, vp, i32, i32, vp, vp, vp, vp]),
         "tf_kappa_residual_f64": (i32, [G, O, vp, vp, vp, i32, vp, vp, vp, vp]),

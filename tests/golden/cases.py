@@ -153,3 +153,45 @@ SWEEP_CASES = {
     "sw_electrode": ("electrode", lambda: random_labels((2, 13, 10, 12), 18), {}, 57),
     "sw_periodic_electrode": ("periodic_electrode", lambda: random_labels((12, 10, 14), 19), {}, 57),
 }
+
+
+def _imp_deadend(n=100):
+    img = np.zeros((n, n))
+    img[:75, 45:55] = 1
+    return img
+
+
+def _imp_throughpore(n=100):
+    img = np.zeros((n, n))
+    img[:, 45:55] = 1
+    return img
+
+
+def _imp_blob(shape, seed, porosity=0.5, inert=0.0, sigma=1.5):
+    """Label 1 (pore) where a blurred noise field is in its top `porosity` quantile, label 0
+    (solid) elsewhere; with `inert` > 0 a second blurred field turns that fraction of the solid
+    into label 2 (neither conductive nor reactive)."""
+    from scipy.ndimage import gaussian_filter
+
+    rng = np.random.default_rng(seed)
+    f = gaussian_filter(rng.standard_normal(shape), sigma)
+    img = (f > np.quantile(f, 1 - porosity)).astype(np.uint8)
+    if inert:
+        g = gaussian_filter(rng.standard_normal(shape), sigma)
+        img[(g > np.quantile(g, 1 - inert)) & (img == 0)] = 2
+    return img
+
+
+# name -> (periodic y/z, input builder, constructor kwargs, solve kwargs, reference code or test)
+IMPEDANCE_CASES = {
+    "imp_deadend": (False, _imp_deadend, {}, {}, "tests/test_taufactor.py:253-259"),
+    "imp_throughpore": (False, _imp_throughpore, {}, {}, "tests/test_taufactor.py:261-267"),
+    "imp_blob": (False, lambda: _imp_blob((20, 14, 12), 1), {}, {}, "electrode.py:160-351"),
+    "imp_blob3": (False, lambda: _imp_blob((20, 14, 12), 2, inert=0.3), {}, {}, "electrode.py:160-351"),
+    "imp_swap": (False, lambda: _imp_blob((18, 12, 14), 3),
+                 {"conductive_label": 0, "reactive_label": 1, "spacing": 0.5}, {}, "electrode.py:167-176"),
+    "imp_limit": (False, lambda: _imp_blob((18, 12, 10), 7), {}, {"iter_limit": 150}, "electrode.py:302-314"),
+    "imp_nyquist": (False, lambda: _imp_blob((8, 6, 6), 4), {"mode": "nyquist"}, {}, "electrode.py:192-197"),
+    "pimp_blob": (True, lambda: _imp_blob((16, 12, 10), 5), {}, {}, "electrode.py:369-402"),
+    "pimp_odd": (True, lambda: _imp_blob((14, 9, 11), 6, inert=0.2), {}, {}, "electrode.py:369-402"),
+}

@@ -2,13 +2,19 @@
 
 Usage (needs the reference source tree; see oracle/ref_shim.py):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py              # reference_outputs.npz
+    python tests/golden/make_golden.py impedance    # impedance_outputs.npz
 
 For every case in ``cases.SOLVE_CASES`` the reference solver class is built with
 ``device='cpu'`` and ``solve(verbose=False, **solve_kwargs)`` is run; tau, D_eff, the iteration
 count, the convergence flag and the layer arrays (flux_1d, c_x, tau_x) are stored. For every
 case in ``cases.SWEEP_CASES`` the reference loop body (taufactor/taufactor.py:175-182) is run the
 given number of times and the padded float32 field is stored bit for bit.
+
+For every case in ``cases.IMPEDANCE_CASES`` the reference's ``ImpedanceSolver`` or
+``PeriodicImpedanceSolver`` (taufactor/electrode.py:160-402) is built with ``device='cpu'`` and
+solved; its set-up arrays, per-frequency taus, impedances and convergence flags, the summed
+iteration count and the final complex128 field go to ``impedance_outputs.npz``.
 """
 from __future__ import annotations
 
@@ -23,7 +29,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
 sys.path.insert(0, HERE)
 
-from cases import SOLVE_CASES, SWEEP_CASES  # noqa: E402
+from cases import IMPEDANCE_CASES, SOLVE_CASES, SWEEP_CASES  # noqa: E402
 from oracle.ref_shim import import_reference  # noqa: E402
 
 CLASS_OF = {
@@ -92,5 +98,34 @@ def main():
     np.savez_compressed(os.path.join(HERE, "reference_outputs.npz"), **out)
 
 
+def impedance_main():
+    tau = import_reference()
+    if tau is None:
+        raise SystemExit("reference source tree not found")
+    out = {}
+    for name, (periodic, make, kw, solve_kw, _src) in IMPEDANCE_CASES.items():
+        img = make()
+        cls = tau.PeriodicImpedanceSolver if periodic else tau.ImpedanceSolver
+        with contextlib.redirect_stdout(io.StringIO()):
+            s = cls(img, device="cpu", **kw)
+            s.solve(verbose=False, **solve_kw)
+        out[f"{name}/taus"] = np.array([float(np.asarray(t)[0]) for t in s.taus])
+        out[f"{name}/impedance"] = np.array(s.impedance, dtype=np.complex128)
+        out[f"{name}/converged_freq"] = np.array(s.converged_freq, dtype=bool)
+        out[f"{name}/sum_iter"] = np.asarray(s.sum_iter)
+        out[f"{name}/field"] = s.field.numpy()[0].copy()
+        out[f"{name}/c_x"] = np.asarray(s.c_x, dtype=np.float64)
+        out[f"{name}/vol_x"] = np.asarray(s.vol_x)
+        out[f"{name}/a_x"] = np.asarray(s.a_x)
+        out[f"{name}/freq_0"] = np.asarray(s.freq_0)
+        out[f"{name}/frequency"] = np.asarray(s.frequency)
+        out[f"{name}/Z_mean"] = np.asarray(s.Z_mean)
+        print(f"{name:18s} sum_iter={s.sum_iter:6d} taus={out[name + '/taus'][:3]}")
+    np.savez_compressed(os.path.join(HERE, "impedance_outputs.npz"), **out)
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["impedance"]:
+        impedance_main()
+    else:
+        main()
