@@ -273,6 +273,7 @@ extern "C" int tf_impedance_sweep(int n_freq, int nx, int ny, int nz, int period
     int bx = 1;
     while (bx < hz && bx < 64) bx <<= 1;
     const dim3 block(bx, 256 / bx);
+    if ((ny + (int)block.y - 1) / (int)block.y > 65535) return TF_ERR_UNSUPPORTED;
     const long long planes = (long long)n_freq * nx;
     const dim3 grid((hz + bx - 1) / bx, (ny + block.y - 1) / block.y, (unsigned)(planes < 65535 ? planes : 65535));
     const int per_plane = 2 * (nz + 2) + 2 * ny;
