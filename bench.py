@@ -552,9 +552,12 @@ def impedance_throughput(dev, side=256, nyq_side=64, cpu_half_sweeps=4):
     r = b.solve_frequencies()
     torch.cuda.synchronize()
     t_bat = time.perf_counter() - t3
-    ok = np.isfinite(r["impedance"]) & np.array([np.isfinite(z) for z in a.impedance])
-    agree = [abs(complex(a.impedance[k]) - r["impedance"][k]) / abs(r["impedance"][k])
-             for k in np.flatnonzero(ok) if a.converged_freq[k] and r["converged"][k]]
+    # frequencies that both runs converged with a finite, non-zero tau (a NaN field ends a
+    # frequency with tau = inf and its impedance left at 0)
+    seq_tau = np.array([float(np.asarray(v)[0]) for v in a.taus])
+    both = (np.array(a.converged_freq) & r["converged"] & np.isfinite(seq_tau) & (seq_tau != 0)
+            & np.isfinite(r["tau"]) & (r["tau"] != 0))
+    agree = [abs(complex(a.impedance[k]) - r["impedance"][k]) / abs(r["impedance"][k]) for k in np.flatnonzero(both)]
     return {"workload": f"ImpedanceSolver {side}^3 pore volume (porosity 0.45, sigma 2, rng 5000; isolated pores inert)",
             "dtype": "complex128", "half_sweeps": int(s.sum_iter), "converged_freq": s.converged_freq,
             "taus": [float(np.asarray(v)[0]) for v in s.taus], "solve_s": t, "voxel_updates_per_s": vu / t,
@@ -567,6 +570,7 @@ def impedance_throughput(dev, side=256, nyq_side=64, cpu_half_sweeps=4):
                         "sequential_converged": int(sum(a.converged_freq)),
                         "side_by_side_s": t_bat, "side_by_side_half_sweeps": [int(v) for v in r["iters"]],
                         "side_by_side_converged": int(r["converged"].sum()),
+                        "both_converged_finite": int(both.sum()),
                         "max_rel_diff_converged": float(max(agree)) if agree else None}}
 
 
@@ -676,6 +680,18 @@ def run_profile(args):
     import taufactor_gb300 as tg
     from taufactor_gb300.synthetic import batch_256
 
+    if args.impedance:  # ImpedanceSolver on one --side^3 pore volume (impedance_volume, seed 5000)
+        s = tg.ImpedanceSolver(impedance_volume(args.side, 5000), device="cuda")
+        s.frc = s.frequency[0]
+        s.field = s.init_field_internal()
+        s._set_factor(s.frc)
+        s._advance(8)
+        torch.cuda.synchronize()
+        s._advance(args.half_sweeps)
+        s._reduce()
+        torch.cuda.synchronize()
+        print(f"profile workload done: impedance {args.side}^3, {args.half_sweeps} half-sweeps")
+        return
     vols = batch_256(args.batch, args.side, SIGMA)
     cls = tg.PeriodicSolver if args.periodic else tg.Solver
     s = cls(vols, device="cuda")
@@ -701,6 +717,7 @@ def main():
     ap.add_argument("--side", type=int, default=256, help="--profile: volume side")
     ap.add_argument("--half-sweeps", type=int, default=40, help="--profile: half-sweeps")
     ap.add_argument("--periodic", action="store_true", help="--profile: PeriodicSolver")
+    ap.add_argument("--impedance", action="store_true", help="--profile: ImpedanceSolver on one volume")
     ap.add_argument("--workload", choices=["uneven", "adjoint", "design", "electrode", "impedance"], default=None,
                     help="print the secondary measurement of this workload only")
     ap.add_argument("--fd-voxels", type=int, default=0, help="--workload adjoint: finite-difference check")

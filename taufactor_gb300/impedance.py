@@ -138,6 +138,15 @@ class ImpedanceSolver(SORSolver):
 
     # ------------------------------------------------------------ reference surface
     @property
+    def field(self):
+        """The solver's complex128 field [1, Nx+2, Ny+2, Nz+2] on the device (None before solve)."""
+        return self._field
+
+    @field.setter
+    def field(self, value):
+        self._field = value
+
+    @property
     def mask(self) -> torch.Tensor:
         """float64 [1, Nx, Ny, Nz] conductive mask (electrode.py:181-182)."""
         return (self._code >> 7).to(torch.float64)[None]
