@@ -4,8 +4,10 @@ The reference batches only volumes of one shape along a leading axis, and the wh
 iterates until its slowest member converges (taufactor/taufactor.py:30-31, :143). Here every
 volume keeps its own shape, buffers and convergence state:
 
-* one launch of the fused sweep advances all still-active volumes by 4 half-sweeps (CTAs of
-  converged volumes return at once);
+* one launch of the fused sweep advances all still-active volumes by 4 half-sweeps; its work
+  list (tile columns split into x-chunks) holds only the volumes still active when the host
+  last looked, and when few remain their chunks get shorter so that they still spread over the
+  SMs (a volume's result does not depend on how its columns are chunked);
 * every 100 half-sweeps the per-volume layer sums and the reference's convergence decision
   (taufactor.py:109-153, :293-331) run on the device and set a per-volume status;
 * two such check intervals (50 sweep launches, two layer-sum and two decision launches) are
@@ -35,6 +37,8 @@ from .solvers import layer_metrics
 
 INTERVAL = 100  # half-sweeps between convergence checks (taufactor.py:184-185)
 CHUNK = 32  # planes per work item of the batched sweep
+MIN_CHUNK = 8  # shortest x-chunk when few volumes remain (each chunk streams 2 K extra planes)
+RECOMPACT = 0.75  # rebuild the work list (and re-capture the graph) below this share of items
 
 
 def _ptr(t: torch.Tensor) -> int:
@@ -92,7 +96,7 @@ class BatchSolve:
         ty, tz, kk = C.c_int(), C.c_int(), C.c_int()
         lib.tf_batch_tile(C.byref(ty), C.byref(tz), C.byref(kk))
         self.k = kk.value
-        work, planes = [], []
+        self._nx, self._tiles = [], []
         flux_off, csum_off, d_mean = [], [], []
         nf = nc = 0
         with torch.cuda.device(self.device):
@@ -132,21 +136,16 @@ class BatchSolve:
                 self.fa.append(fa)
                 self.fb.append(fb)
                 self.codes.append(code)
-                tiles = ((ny + ty.value - 1) // ty.value) * ((nz + tz.value - 1) // tz.value)
-                # x-chunks of about CHUNK planes: items of large and small volumes take about
-                # equally long, so a launch does not wait on the longest columns
-                nch = max(1, round(nx / CHUNK))
-                bounds = [(c * nx) // nch for c in range(nch + 1)]
-                work += [(v, t, bounds[c], bounds[c + 1]) for t in range(tiles) for c in range(nch)]
-                planes += [(v, x) for x in range(nx)]
+                self._tiles.append(((ny + ty.value - 1) // ty.value) * ((nz + tz.value - 1) // tz.value))
+                self._nx.append(nx)
                 flux_off.append(nf)
                 csum_off.append(nc)
                 nf += max(nx - 1, 1)
                 nc += nx
                 d_mean.append(float(res.D_mean[0]))
-            self.work = torch.tensor(work, dtype=torch.int32, device=self.device).reshape(-1)
-            self.planes = torch.tensor(planes, dtype=torch.int32, device=self.device).reshape(-1)
-            self.n_work, self.n_planes = len(work), len(planes)
+            self._sms = torch.cuda.get_device_properties(self.device).multi_processor_count
+            self._work_cache, self._plane_cache = {}, {}
+            self._set_work(tuple(range(n)))
             self.flux = torch.zeros(nf, dtype=torch.float64, device=self.device)
             self.csum = torch.zeros(nc, dtype=torch.float64, device=self.device)
             self.flux_off, self.csum_off = flux_off, csum_off
@@ -179,6 +178,56 @@ class BatchSolve:
 
     def _stream(self):
         return torch.cuda.current_stream(self.device).cuda_stream
+
+    # ---------------------------------------------------------------- work lists
+    def _work_for(self, vols):
+        """Work items (volume, tile, x0, x1) of the volumes `vols`, int32 on the device, and their
+        number. Columns split into x-chunks of about CHUNK planes, so that items of large and
+        small volumes take about equally long; when the items would not fill the SMs twice over,
+        the chunks shrink (down to MIN_CHUNK planes) to spread the remaining volumes."""
+        key = tuple(int(v) for v in vols)
+        hit = self._work_cache.get(key)
+        if hit is not None:
+            return hit
+        base = [max(1, round(self._nx[v] / CHUNK)) for v in key]
+        total = sum(b * self._tiles[v] for b, v in zip(base, key))
+        target = 2 * self._sms
+        items = []
+        for b, v in zip(base, key):
+            nx, nch = self._nx[v], b
+            if 0 < total < target:
+                nch = min(max(1, nx // MIN_CHUNK), -(-b * target // total))
+            bounds = [(c * nx) // nch for c in range(nch + 1)]
+            items += [(v, t, bounds[c], bounds[c + 1]) for t in range(self._tiles[v]) for c in range(nch)]
+        w = torch.tensor(items, dtype=torch.int32, device=self.device).reshape(-1)
+        self._work_cache[key] = (w, len(items))
+        return w, len(items)
+
+    def _planes_for(self, vols):
+        key = tuple(int(v) for v in vols)
+        hit = self._plane_cache.get(key)
+        if hit is None:
+            planes = [(v, x) for v in key for x in range(self._nx[v])]
+            hit = (torch.tensor(planes, dtype=torch.int32, device=self.device).reshape(-1), len(planes))
+            self._plane_cache[key] = hit
+        return hit
+
+    def _set_work(self, vols):
+        self.work, self.n_work = self._work_for(vols)
+        self.planes, self.n_planes = self._planes_for(vols)
+        self._work_vols = set(int(v) for v in vols)
+
+    def _compact(self, status) -> bool:
+        """Shrink the work list to the active volumes when that drops enough items (or when a
+        volume resumed from a pause is missing from it); True if it changed."""
+        act = tuple(np.flatnonzero(status == TF_BATCH_ACTIVE))
+        if not act:
+            return False
+        w, nw = self._work_for(act)
+        if set(act) <= self._work_vols and nw > RECOMPACT * self.n_work:
+            return False
+        self._set_work(act)
+        return True
 
     # ---------------------------------------------------------------- device steps
     def _interval(self, interval: int, start_in_b: int, conv_crit: float):
@@ -243,6 +292,8 @@ class BatchSolve:
         start = timer()
         self.c64 = None
         with torch.cuda.device(self.device):
+            if self._compact(self.status.cpu().numpy()):
+                self.graph = None
             if graph and self.graph is None:
                 self.graph = self._capture(conv_crit)
                 self._graph_crit = conv_crit
@@ -266,6 +317,8 @@ class BatchSolve:
                     print(f"half-sweeps {it}: {int((status == TF_BATCH_ACTIVE).sum())} of {self.n} active")
                 if not (status == TF_BATCH_ACTIVE).any():
                     break
+                if self._compact(status) and graph:
+                    self.graph = self._capture(conv_crit)
             if int(self.err.item()):
                 raise _capi.TfError(int(self.err.item()), "tf_batch_advance (device)")
             self._collect(it)
@@ -365,8 +418,9 @@ class BatchSolve:
                     self.fa[v].zero_()
                 self._launches = torch.tensor(launches, dtype=torch.int32).to(self.device)
                 for j in range(max(launches)):
-                    check(lib.tf_batch_advance_rhs(_ptr(self.desc_rhs), _ptr(self.work), self.n_work,
-                                                   _ptr(self._launches), j, st), "tf_batch_advance_rhs")
+                    w, nw = self._work_for([v for v in range(n) if launches[v] > j])
+                    check(lib.tf_batch_advance_rhs(_ptr(self.desc_rhs), _ptr(w), nw, _ptr(self._launches), j, st),
+                          "tf_batch_advance_rhs")
                 for v in np.nonzero(active)[0]:
                     check(lib.tf_axpy_f64(C.byref(self.geoms[v]), _ptr(c64[v]), _ptr(self.fa[v]), st), "tf_axpy_f64")
             if int(self.err.item()):

@@ -58,6 +58,28 @@ def test_batch_x_chunks_match_single_volume_solvers(monkeypatch):
     assert all(r.residual_history[-1] < 1e-10 for r in res)
 
 
+def test_batch_short_chunks_and_compaction_match_single_volume_solvers(monkeypatch):
+    """Chunks shorter than the fused depth (down to 1 plane) and work lists compacted as volumes
+    converge give the single-volume results bit for bit."""
+    import taufactor_gb300.batch as batch_mod
+
+    monkeypatch.setattr(batch_mod, "CHUNK", 6)
+    monkeypatch.setattr(batch_mod, "MIN_CHUNK", 1)
+    vols, periodic = _volumes()
+    b = tg.BatchSolve(vols, periodic=periodic)
+    n0 = b.n_work
+    res = b.solve(conv_crit=1e-3, poll=1)
+    assert len(b._work_cache) > 1 and b.n_work < n0  # the list shrank as volumes converged
+    for v, (img, per) in enumerate(zip(vols, periodic)):
+        s = (tg.PeriodicSolver if per else tg.Solver)(img)
+        s.solve(verbose=False, conv_crit=1e-3)
+        assert res[v].iter == s.iter
+        np.testing.assert_allclose(res[v].D_eff, s.D_eff, rtol=1e-12)
+        assert np.array_equal(b.field(v).cpu().numpy()[:, :, 1:-1, 1:-1], s.field.cpu().numpy()[:, :, 1:-1, 1:-1])
+    res = b.refine(tol=1e-10)
+    assert all(r.residual_history[-1] < 1e-10 for r in res)
+
+
 def test_batch_non_percolating_volume():
     vols, periodic = _volumes()
     dead = np.zeros((20, 16, 32), dtype=np.uint8)
