@@ -205,13 +205,16 @@ typedef struct tf_batch_state { /* device arrays of n_vol entries unless noted *
 /* Bytes of the device descriptor table for n_vol volumes. */
 size_t tf_batch_desc_bytes(int n_vol);
 
-/* Tile shape and half-sweeps per launch of the batched sweep. */
+/* Tile shape of tile class 0 (class 1: tile_z = 128; class 2: tile_y = 32) and half-sweeps per
+ * launch of the batched sweep. */
 void tf_batch_tile(int* tile_y, int* tile_z, int* half_sweeps);
 
 /* Fill the descriptor table (device memory, tf_batch_desc_bytes) from per-volume geometry,
  * operator, buffers (field A holds the current field), layer-sum offsets (flux arena offset of
  * plane 0; csum arena likewise) and mean conductive fraction d_mean (tau = d_mean / D_rel).
- * Synchronous (copies the table to the device). */
+ * ops[v].tile picks the volume's tile class (rows x z-cells): 1 = 16 x 128, 2 = 32 x 64,
+ * otherwise 16 x 64; a volume's work items go to the launches of its class. Synchronous (copies the table to the
+ * device). */
 int tf_batch_describe(int n_vol, const tf_geom* geoms, const tf_operator* ops, float* const* field_a,
                       float* const* field_b, const uint8_t* const* codes, const int64_t* flux_off,
                       const int64_t* csum_off, const double* d_mean, int32_t* err_dev, void* desc_dev);
@@ -228,6 +231,9 @@ int tf_batch_describe_rhs(int n_vol, const tf_geom* geoms, const tf_operator* op
  * count so that its result ends in field A). Launch parity selects A -> B or B -> A. */
 int tf_batch_advance_rhs(const void* desc_dev, const int32_t* work_dev, int n_work, const int32_t* launches_dev,
                          int launch, void* stream);
+/* The same for the work items of tile class `tile` (0..2); tf_batch_advance_rhs is class 0. */
+int tf_batch_advance_rhs_tile(const void* desc_dev, const int32_t* work_dev, int n_work,
+                              const int32_t* launches_dev, int launch, int tile, void* stream);
 
 /* Advance every active volume by the batch's half-sweeps per launch (colour 0 first, so the
  * completed half-sweeps must stay a multiple of it). work_dev: int32 quads (volume, tile, x0, x1)
@@ -236,6 +242,11 @@ int tf_batch_advance_rhs(const void* desc_dev, const int32_t* work_dev, int n_wo
  * reverse. */
 int tf_batch_advance(const void* desc_dev, const int32_t* work_dev, int n_work, const int32_t* status_dev,
                      int parity, void* stream);
+/* The same for the work items of tile class `tile` (0..2); tf_batch_advance is class 0. Items
+ * of volumes of the other class return at once. The two classes' volumes are independent, so
+ * their launches may run on different streams between two layer-sum / check steps. */
+int tf_batch_advance_tile(const void* desc_dev, const int32_t* work_dev, int n_work, const int32_t* status_dev,
+                          int parity, int tile, void* stream);
 
 /* Per-plane float64 flux / field sums of every active volume (tf_layer_sums per volume) into
  * the arenas; planes_dev: int32 pairs (volume, x). cur_in_b: the current fields are in B. */

@@ -4,10 +4,13 @@ The reference batches only volumes of one shape along a leading axis, and the wh
 iterates until its slowest member converges (taufactor/taufactor.py:30-31, :143). Here every
 volume keeps its own shape, buffers and convergence state:
 
-* one launch of the fused sweep advances all still-active volumes by 4 half-sweeps; its work
-  list (tile columns split into x-chunks) holds only the volumes still active when the host
-  last looked, and when few remain their chunks get shorter so that they still spread over the
-  SMs (a volume's result does not depend on how its columns are chunked);
+* one launch of the fused sweep per tile class advances all still-active volumes by 4
+  half-sweeps; volumes whose z-extent is a multiple of 128 use 16 x 128 tiles, those whose
+  y-extent is a multiple of 32 use 32 x 64, the others 16 x 64 (rows x z-cells), and the
+  classes run on their own streams between checks. A work list (tile columns
+  split into x-chunks) holds only the volumes still active when the host last looked, and when
+  few remain their chunks get shorter so that they still spread over the SMs (a volume's result
+  does not depend on its tile class or on how its columns are chunked);
 * every 100 half-sweeps the per-volume layer sums and the reference's convergence decision
   (taufactor.py:109-153, :293-331) run on the device and set a per-volume status;
 * two such check intervals (50 sweep launches, two layer-sum and two decision launches) are
@@ -96,7 +99,7 @@ class BatchSolve:
         ty, tz, kk = C.c_int(), C.c_int(), C.c_int()
         lib.tf_batch_tile(C.byref(ty), C.byref(tz), C.byref(kk))
         self.k = kk.value
-        self._nx, self._tiles = [], []
+        self._nx, self._tiles, self._cls = [], [], []
         flux_off, csum_off, d_mean = [], [], []
         nf = nc = 0
         with torch.cuda.device(self.device):
@@ -119,6 +122,10 @@ class BatchSolve:
                 op = self.ops[v]
                 op.kind = TF_KIND_BINARY
                 op.periodic = pflag
+                # tile class (rows x z-cells): 16 x 128 where it covers the z-extent exactly, else
+                # 32 x 64 where that covers the y-extent, else 16 x 64
+                cls = 1 if nz % (2 * tz.value) == 0 else (2 if ny % (2 * ty.value) == 0 else 0)
+                op.tile = cls
                 w = om[v] if om[v] is not None else 2 - math.pi / (1.5 * nx)
                 op.omega = float(np.float32(w))
                 op.ghost_lo, op.ghost_hi = 2 * res.top_bc, 2 * res.bot_bc
@@ -136,8 +143,10 @@ class BatchSolve:
                 self.fa.append(fa)
                 self.fb.append(fb)
                 self.codes.append(code)
-                self._tiles.append(((ny + ty.value - 1) // ty.value) * ((nz + tz.value - 1) // tz.value))
+                tyc, tzc = ty.value * (2 if cls == 2 else 1), tz.value * (2 if cls == 1 else 1)
+                self._tiles.append(((ny + tyc - 1) // tyc) * ((nz + tzc - 1) // tzc))
                 self._nx.append(nx)
+                self._cls.append(cls)
                 flux_off.append(nf)
                 csum_off.append(nc)
                 nf += max(nx - 1, 1)
@@ -146,6 +155,7 @@ class BatchSolve:
             self._sms = torch.cuda.get_device_properties(self.device).multi_processor_count
             self._work_cache, self._plane_cache = {}, {}
             self._set_work(tuple(range(n)))
+            self._side = [None, torch.cuda.Stream(self.device), torch.cuda.Stream(self.device)]  # classes 1, 2
             self.flux = torch.zeros(nf, dtype=torch.float64, device=self.device)
             self.csum = torch.zeros(nc, dtype=torch.float64, device=self.device)
             self.flux_off, self.csum_off = flux_off, csum_off
@@ -181,10 +191,11 @@ class BatchSolve:
 
     # ---------------------------------------------------------------- work lists
     def _work_for(self, vols):
-        """Work items (volume, tile, x0, x1) of the volumes `vols`, int32 on the device, and their
-        number. Columns split into x-chunks of about CHUNK planes, so that items of large and
-        small volumes take about equally long; when the items would not fill the SMs twice over,
-        the chunks shrink (down to MIN_CHUNK planes) to spread the remaining volumes."""
+        """Work items (volume, tile, x0, x1) of the volumes `vols` per tile class: a pair of
+        (int32 device tensor or None, count). Columns split into x-chunks of about CHUNK planes,
+        so that items of large and small volumes take about equally long; when the items would
+        not fill the SMs twice over, the chunks shrink (down to MIN_CHUNK planes) to spread the
+        remaining volumes."""
         key = tuple(int(v) for v in vols)
         hit = self._work_cache.get(key)
         if hit is not None:
@@ -192,16 +203,18 @@ class BatchSolve:
         base = [max(1, round(self._nx[v] / CHUNK)) for v in key]
         total = sum(b * self._tiles[v] for b, v in zip(base, key))
         target = 2 * self._sms
-        items = []
+        items = ([], [], [])
         for b, v in zip(base, key):
             nx, nch = self._nx[v], b
             if 0 < total < target:
                 nch = min(max(1, nx // MIN_CHUNK), -(-b * target // total))
             bounds = [(c * nx) // nch for c in range(nch + 1)]
-            items += [(v, t, bounds[c], bounds[c + 1]) for t in range(self._tiles[v]) for c in range(nch)]
-        w = torch.tensor(items, dtype=torch.int32, device=self.device).reshape(-1)
-        self._work_cache[key] = (w, len(items))
-        return w, len(items)
+            items[self._cls[v]].extend((v, t, bounds[c], bounds[c + 1]) for t in range(self._tiles[v])
+                                       for c in range(nch))
+        hit = tuple((torch.tensor(it, dtype=torch.int32, device=self.device).reshape(-1) if it else None, len(it))
+                    for it in items)
+        self._work_cache[key] = hit
+        return hit
 
     def _planes_for(self, vols):
         key = tuple(int(v) for v in vols)
@@ -213,18 +226,19 @@ class BatchSolve:
         return hit
 
     def _set_work(self, vols):
-        self.work, self.n_work = self._work_for(vols)
+        self.works = self._work_for(vols)
+        self.n_work = sum(nw for _, nw in self.works)
         self.planes, self.n_planes = self._planes_for(vols)
         self._work_vols = set(int(v) for v in vols)
 
     def _compact(self, status) -> bool:
-        """Shrink the work list to the active volumes when that drops enough items (or when a
-        volume resumed from a pause is missing from it); True if it changed."""
+        """Shrink the work lists to the active volumes when that drops enough items (or when a
+        volume resumed from a pause is missing from them); True if they changed."""
         act = tuple(np.flatnonzero(status == TF_BATCH_ACTIVE))
         if not act:
             return False
-        w, nw = self._work_for(act)
-        if set(act) <= self._work_vols and nw > RECOMPACT * self.n_work:
+        w = self._work_for(act)
+        if set(act) <= self._work_vols and sum(nw for _, nw in w) > RECOMPACT * self.n_work:
             return False
         self._set_work(act)
         return True
@@ -233,11 +247,21 @@ class BatchSolve:
     def _interval(self, interval: int, start_in_b: int, conv_crit: float):
         """100 half-sweeps of every active volume, then layer sums and the decision."""
         lib, st = self.lib, self._stream()
+        main = torch.cuda.current_stream(self.device)
+        # classes 1 and 2 sweep on their own streams meanwhile (volumes are independent)
+        side = [c for c in (1, 2) if self.works[c][1]]
+        for c in side:
+            self._side[c].wait_stream(main)
         parity = start_in_b
         for _ in range(INTERVAL // self.k):
-            check(lib.tf_batch_advance(_ptr(self.desc), _ptr(self.work), self.n_work, _ptr(self.status), parity, st),
-                  "tf_batch_advance")
+            for c, (w, nw) in enumerate(self.works):
+                if nw:
+                    stream = st if c == 0 else self._side[c].cuda_stream
+                    check(lib.tf_batch_advance_tile(_ptr(self.desc), _ptr(w), nw, _ptr(self.status), parity, c,
+                                                    stream), "tf_batch_advance_tile")
             parity ^= 1
+        for c in side:
+            main.wait_stream(self._side[c])
         check(lib.tf_batch_layer_sums(_ptr(self.desc), _ptr(self.planes), self.n_planes, _ptr(self.status), parity,
                                       _ptr(self.flux), _ptr(self.csum), st), "tf_batch_layer_sums")
         check(lib.tf_batch_check(_ptr(self.desc), self.n, _ptr(self.flux), self.state, float(conv_crit), interval,
@@ -418,9 +442,11 @@ class BatchSolve:
                     self.fa[v].zero_()
                 self._launches = torch.tensor(launches, dtype=torch.int32).to(self.device)
                 for j in range(max(launches)):
-                    w, nw = self._work_for([v for v in range(n) if launches[v] > j])
-                    check(lib.tf_batch_advance_rhs(_ptr(self.desc_rhs), _ptr(w), nw, _ptr(self._launches), j, st),
-                          "tf_batch_advance_rhs")
+                    for cls, (w, nw) in enumerate(self._work_for([v for v in range(n) if launches[v] > j])):
+                        if nw:
+                            check(lib.tf_batch_advance_rhs_tile(_ptr(self.desc_rhs), _ptr(w), nw,
+                                                                _ptr(self._launches), j, cls, st),
+                                  "tf_batch_advance_rhs_tile")
                 for v in np.nonzero(active)[0]:
                     check(lib.tf_axpy_f64(C.byref(self.geoms[v]), _ptr(c64[v]), _ptr(self.fa[v]), st), "tf_axpy_f64")
             if int(self.err.item()):

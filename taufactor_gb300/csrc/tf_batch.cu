@@ -6,7 +6,11 @@
 // k_stream_multi launch advances every still-active volume by K half-sweeps: CTA w takes work
 // item (volume, tile, x0, x1) from a table and runs the same per-tile body as the single-volume
 // kernel on planes [x0, x1) of that tile column (x-chunks keep the items of large and small
-// volumes about equally long); CTAs of volumes whose status is not "active" return at once. k_layer_sums_multi and
+// volumes about equally long); CTAs of volumes whose status is not "active" return at once.
+// Volumes come in three tile classes (rows x z-cells: 0 = 16 x 64, 1 = 16 x 128, 2 = 32 x 64),
+// each with its own kernel instantiation and work list; the class is the volume's
+// tf_operator.tile.
+// k_layer_sums_multi and
 // k_batch_check then evaluate the reference's convergence rule (taufactor.py:109-153,
 // :293-331) per volume on the device and set its status, so a whole check interval -- sweeps,
 // layer sums, decision -- runs without the host and can be captured in a CUDA graph.
@@ -24,20 +28,27 @@
 
 namespace tf {
 
-constexpr int BTY = 16, BTZ = 64, BK = 4;  // tile and fused depth of the batched sweep
+constexpr int BTY = 16, BTZ = 64, BK = 4;  // tile (class 0) and fused depth of the batched sweep
+constexpr int BTZ1 = 128;                  // z-cells of a class-1 tile (16 rows)
+constexpr int BTY2 = 32;                   // rows of a class-2 tile (64 z-cells)
 using BShape = StreamShape<BTY, BTZ, BK>;
+using BShape1 = StreamShape<BTY, BTZ1, BK>;
+using BShape2 = StreamShape<BTY2, BTZ, BK>;
 
 struct alignas(64) VolDesc {
-    CUtensorMap map_a, map_b, map_c;  // field A, field B, codes
+    CUtensorMap map_a, map_b, map_c;  // field A, field B, codes (boxes of the volume's tile class)
     SweepArgs ab, ba;                 // A -> B and B -> A
     const uint8_t* code;
     int tiles_z, tiles_y;
+    int tile_y, tile_z;               // rows and z-cells of the volume's tiles (its class)
     long long flux_off, csum_off;  // offsets into the layer-sum arenas
     double d_mean;                 // mean conductive fraction (tau = d_mean / D_rel)
     double inv_area;               // 1 / (ny * nz)
 };
 
-__global__ void __launch_bounds__(BShape::NT, 2)
+// Work items of volumes of another tile class (a caller's mix-up) return without touching them.
+template <int TY, int TZ>
+__global__ void __launch_bounds__(StreamShape<TY, TZ, BK>::NT, StreamShape<TY, TZ, BK>::NT <= 256 ? 2 : 1)
     k_stream_multi(const VolDesc* __restrict__ desc, const int4* __restrict__ work,
                    const int32_t* __restrict__ status, int parity) {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -45,15 +56,17 @@ __global__ void __launch_bounds__(BShape::NT, 2)
     const int v = item.x;
     if (status[v] != TF_BATCH_ACTIVE) return;
     const VolDesc* d = desc + v;
+    if (d->tile_y != TY || d->tile_z != TZ) return;
     const int tz = item.y % d->tiles_z, ty = item.y / d->tiles_z;
     const SweepArgs a = parity ? d->ba : d->ab;
-    stream_tile<TF_KIND_BINARY, BTY, BTZ, BK, false>(parity ? &d->map_b : &d->map_a, &d->map_c, a, nullptr,
-                                                     tz * (BTZ / 2), ty * BTY, 0, item.z, item.w, smem);
+    stream_tile<TF_KIND_BINARY, TY, TZ, BK, false>(parity ? &d->map_b : &d->map_a, &d->map_c, a, nullptr,
+                                                   tz * (TZ / 2), ty * TY, 0, item.z, item.w, smem);
 }
 
 // Correction sweeps: launch `launch` of an inner solve; volume v takes part while
 // launch < launches[v] (an even count, so each volume's result ends in buffer A).
-__global__ void __launch_bounds__(BShape::NT, 2)
+template <int TY, int TZ>
+__global__ void __launch_bounds__(StreamShape<TY, TZ, BK>::NT, StreamShape<TY, TZ, BK>::NT <= 256 ? 2 : 1)
     k_stream_multi_rhs(const VolDesc* __restrict__ desc, const int4* __restrict__ work,
                        const int32_t* __restrict__ launches, int launch) {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -61,11 +74,12 @@ __global__ void __launch_bounds__(BShape::NT, 2)
     const int v = item.x;
     if (launch >= launches[v]) return;
     const VolDesc* d = desc + v;
+    if (d->tile_y != TY || d->tile_z != TZ) return;
     const int tz = item.y % d->tiles_z, ty = item.y / d->tiles_z;
     const int parity = launch & 1;
     const SweepArgs a = parity ? d->ba : d->ab;
-    stream_tile<TF_KIND_BINARY, BTY, BTZ, BK, true>(parity ? &d->map_b : &d->map_a, &d->map_c, a, nullptr,
-                                                    tz * (BTZ / 2), ty * BTY, 0, item.z, item.w, smem);
+    stream_tile<TF_KIND_BINARY, TY, TZ, BK, true>(parity ? &d->map_b : &d->map_a, &d->map_c, a, nullptr,
+                                                  tz * (TZ / 2), ty * TY, 0, item.z, item.w, smem);
 }
 
 // One CTA per (volume, plane): float64 sums of the masked x-flux through face x|x+1 and of the
@@ -186,31 +200,45 @@ static int describe(int n_vol, const tf_geom* geoms, const tf_operator* ops, flo
         VolDesc& d = h[v];
         std::memset(&d, 0, sizeof(VolDesc));
         const long long planes = (long long)gg.nx;
+        const int cls = op.tile == 1 || op.tile == 2 ? op.tile : 0;
+        const int wj = cls == 1 ? BShape1::WJ : (cls == 2 ? BShape2::WJ : BShape::WJ);
+        const int wjc = cls == 1 ? BShape1::WJC : (cls == 2 ? BShape2::WJC : BShape::WJC);
+        const int rows = cls == 1 ? BShape1::ROWS : (cls == 2 ? BShape2::ROWS : BShape::ROWS);
         int rc = encode_map_3d(&d.map_a, field_a[v], 4, gg.zh, 2 * gg.yp, planes, (long long)gg.zh * 4,
-                               (long long)gg.zh * 4 * 2 * gg.yp, BShape::WJ, 2 * BShape::ROWS);
+                               (long long)gg.zh * 4 * 2 * gg.yp, wj, 2 * rows);
         if (!rc)
             rc = encode_map_3d(&d.map_b, field_b[v], 4, gg.zh, 2 * gg.yp, planes, (long long)gg.zh * 4,
-                               (long long)gg.zh * 4 * 2 * gg.yp, BShape::WJ, 2 * BShape::ROWS);
+                               (long long)gg.zh * 4 * 2 * gg.yp, wj, 2 * rows);
         if (!rc)
             rc = encode_map_3d(&d.map_c, codes[v], 1, gg.zhc, 2 * gg.yp, planes, gg.zhc,
-                               (long long)gg.zhc * 2 * gg.yp, BShape::WJC, 2 * BShape::ROWS);
+                               (long long)gg.zhc * 2 * gg.yp, wjc, 2 * rows);
         if (rc) return rc;
+        d.tile_y = cls == 2 ? BTY2 : BTY;
+        d.tile_z = cls == 1 ? BTZ1 : BTZ;
         const Geo g = make_geo(gg);
         d.ab = make_args(g, op, field_b[v], 0, BK, err_dev);
         d.ba = make_args(g, op, field_a[v], 0, BK, err_dev);
         if (rhs) d.ab.rhs = d.ba.rhs = rhs[v];
         d.code = codes[v];
-        d.tiles_z = (gg.nz + BTZ - 1) / BTZ;
-        d.tiles_y = (gg.ny + BTY - 1) / BTY;
+        d.tiles_z = (gg.nz + d.tile_z - 1) / d.tile_z;
+        d.tiles_y = (gg.ny + d.tile_y - 1) / d.tile_y;
         d.flux_off = flux_off ? flux_off[v] : 0;
         d.csum_off = csum_off ? csum_off[v] : 0;
         d.d_mean = d_mean ? d_mean[v] : 0.0;
         d.inv_area = 1.0 / ((double)gg.ny * gg.nz);
     }
     // kernel attributes are set here, outside any stream capture
-    if (cudaFuncSetAttribute(rhs ? k_stream_multi_rhs : k_stream_multi, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             BShape::SMEM) != cudaSuccess)
-        return TF_ERR_CUDA;
+    const cudaFuncAttribute smem_attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    const bool ok = rhs ? cudaFuncSetAttribute(k_stream_multi_rhs<BTY, BTZ>, smem_attr, BShape::SMEM) == cudaSuccess &&
+                              cudaFuncSetAttribute(k_stream_multi_rhs<BTY, BTZ1>, smem_attr, BShape1::SMEM) ==
+                                  cudaSuccess &&
+                              cudaFuncSetAttribute(k_stream_multi_rhs<BTY2, BTZ>, smem_attr, BShape2::SMEM) ==
+                                  cudaSuccess
+                        : cudaFuncSetAttribute(k_stream_multi<BTY, BTZ>, smem_attr, BShape::SMEM) == cudaSuccess &&
+                              cudaFuncSetAttribute(k_stream_multi<BTY, BTZ1>, smem_attr, BShape1::SMEM) ==
+                                  cudaSuccess &&
+                              cudaFuncSetAttribute(k_stream_multi<BTY2, BTZ>, smem_attr, BShape2::SMEM) == cudaSuccess;
+    if (!ok) return TF_ERR_CUDA;
     return cudaMemcpy(desc_dev, h.data(), sizeof(VolDesc) * n_vol, cudaMemcpyHostToDevice) == cudaSuccess
                ? TF_OK
                : TF_ERR_CUDA;
@@ -237,22 +265,47 @@ int tf_batch_describe_rhs(int n_vol, const tf_geom* geoms, const tf_operator* op
     return describe(n_vol, geoms, ops, field_a, field_b, codes, rhs, nullptr, nullptr, nullptr, err_dev, desc_dev);
 }
 
+int tf_batch_advance_rhs_tile(const void* desc_dev, const int32_t* work_dev, int n_work,
+                              const int32_t* launches_dev, int launch, int tile, void* stream) {
+    if (!desc_dev || !work_dev || n_work <= 0 || !launches_dev || launch < 0 || tile < 0 || tile > 2)
+        return TF_ERR_ARG;
+    const VolDesc* d = static_cast<const VolDesc*>(desc_dev);
+    const int4* w = reinterpret_cast<const int4*>(work_dev);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (tile == 1)
+        k_stream_multi_rhs<BTY, BTZ1><<<n_work, BShape1::NT, BShape1::SMEM, st>>>(d, w, launches_dev, launch);
+    else if (tile == 2)
+        k_stream_multi_rhs<BTY2, BTZ><<<n_work, BShape2::NT, BShape2::SMEM, st>>>(d, w, launches_dev, launch);
+    else
+        k_stream_multi_rhs<BTY, BTZ><<<n_work, BShape::NT, BShape::SMEM, st>>>(d, w, launches_dev, launch);
+    note_launch();
+    return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
+}
+
 int tf_batch_advance_rhs(const void* desc_dev, const int32_t* work_dev, int n_work, const int32_t* launches_dev,
                          int launch, void* stream) {
-    if (!desc_dev || !work_dev || n_work <= 0 || !launches_dev || launch < 0) return TF_ERR_ARG;
-    k_stream_multi_rhs<<<n_work, BShape::NT, BShape::SMEM, (cudaStream_t)stream>>>(
-        static_cast<const VolDesc*>(desc_dev), reinterpret_cast<const int4*>(work_dev), launches_dev, launch);
+    return tf_batch_advance_rhs_tile(desc_dev, work_dev, n_work, launches_dev, launch, 0, stream);
+}
+
+int tf_batch_advance_tile(const void* desc_dev, const int32_t* work_dev, int n_work, const int32_t* status_dev,
+                          int parity, int tile, void* stream) {
+    if (!desc_dev || !work_dev || n_work <= 0 || !status_dev || tile < 0 || tile > 2) return TF_ERR_ARG;
+    const VolDesc* d = static_cast<const VolDesc*>(desc_dev);
+    const int4* w = reinterpret_cast<const int4*>(work_dev);
+    cudaStream_t st = (cudaStream_t)stream;
+    if (tile == 1)
+        k_stream_multi<BTY, BTZ1><<<n_work, BShape1::NT, BShape1::SMEM, st>>>(d, w, status_dev, parity & 1);
+    else if (tile == 2)
+        k_stream_multi<BTY2, BTZ><<<n_work, BShape2::NT, BShape2::SMEM, st>>>(d, w, status_dev, parity & 1);
+    else
+        k_stream_multi<BTY, BTZ><<<n_work, BShape::NT, BShape::SMEM, st>>>(d, w, status_dev, parity & 1);
     note_launch();
     return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
 }
 
 int tf_batch_advance(const void* desc_dev, const int32_t* work_dev, int n_work, const int32_t* status_dev,
                      int parity, void* stream) {
-    if (!desc_dev || !work_dev || n_work <= 0 || !status_dev) return TF_ERR_ARG;
-    k_stream_multi<<<n_work, BShape::NT, BShape::SMEM, (cudaStream_t)stream>>>(
-        static_cast<const VolDesc*>(desc_dev), reinterpret_cast<const int4*>(work_dev), status_dev, parity & 1);
-    note_launch();
-    return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
+    return tf_batch_advance_tile(desc_dev, work_dev, n_work, status_dev, parity, 0, stream);
 }
 
 int tf_batch_layer_sums(const void* desc_dev, const int32_t* planes_dev, int n_planes, const int32_t* status_dev,

@@ -46,7 +46,7 @@ def test_batch_x_chunks_match_single_volume_solvers(monkeypatch):
     monkeypatch.setattr(batch_mod, "CHUNK", 20)
     vols, periodic = _volumes()
     b = tg.BatchSolve(vols, periodic=periodic)
-    assert b.n_work > sum(((s[1] + 15) // 16) * ((s[2] + 63) // 64) for s in SHAPES)
+    assert b.n_work > sum(b._tiles)  # more work items than tile columns: columns are chunked
     res = b.solve(conv_crit=1e-3)
     for v, (img, per) in enumerate(zip(vols, periodic)):
         s = (tg.PeriodicSolver if per else tg.Solver)(img)
@@ -76,6 +76,30 @@ def test_batch_short_chunks_and_compaction_match_single_volume_solvers(monkeypat
         assert res[v].iter == s.iter
         np.testing.assert_allclose(res[v].D_eff, s.D_eff, rtol=1e-12)
         assert np.array_equal(b.field(v).cpu().numpy()[:, :, 1:-1, 1:-1], s.field.cpu().numpy()[:, :, 1:-1, 1:-1])
+    res = b.refine(tol=1e-10)
+    assert all(r.residual_history[-1] < 1e-10 for r in res)
+
+
+def test_batch_tile_classes_match_single_volume_solvers():
+    """Volumes on 16 x 128 tiles (z-extent a multiple of 128) and on 32 x 64 tiles (y-extent a
+    multiple of 32), each class swept on its own stream next to the volumes on 16 x 64 tiles,
+    give the single-volume results bit for bit, with and without the graph, and through the
+    FP64 correction."""
+    shapes = [(32, 32, 128), (24, 48, 64), (28, 16, 256), (36, 64, 96), (20, 32, 72), (30, 40, 96)]
+    vols = [blurred_noise(s, 2.0, 0.55, 400 + i) for i, s in enumerate(shapes)]
+    periodic = [i % 2 == 1 for i in range(len(vols))]
+    for graph in (True, False):
+        b = tg.BatchSolve(vols, periodic=periodic)
+        assert [b.ops[v].tile for v in range(len(vols))] == [1, 0, 1, 2, 2, 0]
+        assert all(nw > 0 for _, nw in b.works)
+        res = b.solve(conv_crit=1e-3, graph=graph)
+        for v, (img, per) in enumerate(zip(vols, periodic)):
+            s = (tg.PeriodicSolver if per else tg.Solver)(img)
+            s.solve(verbose=False, conv_crit=1e-3)
+            assert res[v].iter == s.iter, (v, res[v].iter, s.iter)
+            np.testing.assert_allclose(res[v].D_eff, s.D_eff, rtol=1e-12)
+            assert np.array_equal(b.field(v).cpu().numpy()[:, :, 1:-1, 1:-1],
+                                  s.field.cpu().numpy()[:, :, 1:-1, 1:-1]), v
     res = b.refine(tol=1e-10)
     assert all(r.residual_history[-1] < 1e-10 for r in res)
 

@@ -33,7 +33,7 @@ def test_static_scratch_converge_matches_arena_path():
     from taufactor_gb300._capi import TF_ERR_UNSUPPORTED, check
     from taufactor_gb300.synthetic import blurred_noise
 
-    shapes = [(32, 48, 64), (40, 32, 96), (24, 40, 72)]
+    shapes = [(32, 48, 64), (40, 32, 96), (24, 40, 128)]  # tile classes 0, 2, 1
     vols = [blurred_noise(s, 2.0, 0.55, 300 + i) for i, s in enumerate(shapes)]
     b = tg.BatchSolve(vols, periodic=[False, True, False])
     lib, st = b.lib, b._stream()
@@ -42,8 +42,10 @@ def test_static_scratch_converge_matches_arena_path():
     parity = 0
     for call in range(2):
         for _ in range(25):  # 100 half-sweeps of every volume
-            check(lib.tf_batch_advance(b.desc.data_ptr(), b.work.data_ptr(), b.n_work, b.status.data_ptr(), parity,
-                                       st), "tf_batch_advance")
+            for cls, (w, nw) in enumerate(b.works):
+                if nw:
+                    check(lib.tf_batch_advance_tile(b.desc.data_ptr(), w.data_ptr(), nw, b.status.data_ptr(),
+                                                    parity, cls, st), "tf_batch_advance_tile")
             parity ^= 1
         # the existing path: sums into caller arenas, then the decision
         check(lib.tf_batch_layer_sums(b.desc.data_ptr(), b.planes.data_ptr(), b.n_planes, b.status.data_ptr(),
