@@ -166,6 +166,21 @@ def run_reference(args):
     print(json.dumps(out), flush=True)
 
 
+def combine_ranks(ms: float, units: float, world: int, device=None):
+    """(max over the ranks of the timed region in ms, sum over the ranks of the units they
+    processed); the values themselves at N = 1. Every rank must call it."""
+    if world == 1:
+        return ms, units
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    u = torch.tensor([units], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    dist.all_reduce(u, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(u.item())
+
+
 def run_ours(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -187,8 +202,8 @@ def run_ours(args):
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=dev)
-    vols = batch_256(N_VOL, SIDE, SIGMA)
-    V = vols.size  # voxels in the batch
+    vols = batch_256(N_VOL, SIDE, SIGMA, first=rank * N_VOL)  # each rank its own volumes
+    V = vols.size  # voxels in this rank's batch
 
     def barrier():
         if world > 1:
@@ -221,13 +236,8 @@ def run_ours(args):
         e1.record()
         barrier()
     launches = lib.tf_launch_count() - n0
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        t = torch.tensor([ms], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
     half_sweeps = sum(iters)
-    vu_total = half_sweeps * V / 2 * world
+    ms, vu_total = combine_ranks(e0.elapsed_time(e1), half_sweeps * V / 2, world, dev)
     value = vu_total / (ms / 1e3)
     solves_per_s = N_VOL * args.steps * world / (ms / 1e3)
     d_eff = s.D_eff.copy()
@@ -272,6 +282,8 @@ def run_ours(args):
         pool.close()
         cpu = {"value": rate, "unit": UNIT, "cores": info["cores"], "kind": "port", "sample": info["sample"]}
     if rank != 0:
+        if world > 1:
+            torch.distributed.destroy_process_group()
         return
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

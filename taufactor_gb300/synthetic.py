@@ -20,11 +20,13 @@ def blurred_noise(shape, sigma: float, porosity: float, seed: int) -> np.ndarray
     return (f < thr).astype(np.uint8)
 
 
-def batch_256(n: int = 16, side: int = 256, sigma: float = 2.0, workers: int = 8) -> np.ndarray:
-    """n volumes side^3: volume i from default_rng(1000+i), porosity_i ~ U[0.35,0.70] (default_rng(999))."""
-    por = np.random.default_rng(999).uniform(0.35, 0.70, n)
+def batch_256(n: int = 16, side: int = 256, sigma: float = 2.0, workers: int = 8, first: int = 0) -> np.ndarray:
+    """Volumes first..first+n-1 of one sequence, each side^3: volume i from default_rng(1000+i),
+    porosity_i ~ U[0.35,0.70] (the i-th draw of default_rng(999)). A rank of a multi-GPU run takes
+    its own slice (first = rank * n)."""
+    por = np.random.default_rng(999).uniform(0.35, 0.70, first + n)
     with cf.ThreadPoolExecutor(max_workers=workers) as ex:
-        vols = list(ex.map(lambda i: blurred_noise((side,) * 3, sigma, por[i], 1000 + i), range(n)))
+        vols = list(ex.map(lambda i: blurred_noise((side,) * 3, sigma, por[i], 1000 + i), range(first, first + n)))
     return np.stack(vols)
 
 
