@@ -692,6 +692,16 @@ def run_profile(args):
     import taufactor_gb300 as tg
     from taufactor_gb300.synthetic import batch_256
 
+    if args.uneven:  # one batched solve of the 64 uneven volumes (half periodic)
+        from taufactor_gb300.synthetic import uneven_volumes
+
+        vols = uneven_volumes(64)
+        b = tg.BatchSolve(vols, periodic=[i % 2 == 1 for i in range(len(vols))], device="cuda")
+        b.solve(conv_crit=CONV_CRIT)
+        torch.cuda.synchronize()
+        print(f"profile workload done: uneven batch of {len(vols)} volumes, {max(r.iter for r in b.results)} "
+              "half-sweeps for the slowest")
+        return
     if args.impedance:  # ImpedanceSolver on one --side^3 pore volume (impedance_volume, seed 5000)
         s = tg.ImpedanceSolver(impedance_volume(args.side, 5000), device="cuda")
         s.frc = s.frequency[0]
@@ -730,6 +740,7 @@ def main():
     ap.add_argument("--half-sweeps", type=int, default=40, help="--profile: half-sweeps")
     ap.add_argument("--periodic", action="store_true", help="--profile: PeriodicSolver")
     ap.add_argument("--impedance", action="store_true", help="--profile: ImpedanceSolver on one volume")
+    ap.add_argument("--uneven", action="store_true", help="--profile: one batched solve of the uneven batch")
     ap.add_argument("--workload", choices=["uneven", "adjoint", "design", "electrode", "impedance"], default=None,
                     help="print the secondary measurement of this workload only")
     ap.add_argument("--fd-voxels", type=int, default=0, help="--workload adjoint: finite-difference check")
