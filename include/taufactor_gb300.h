@@ -88,6 +88,14 @@ int64_t tf_launch_count(void);
  * Pure host arithmetic. `periodic` selects which shapes the tiled kernel accepts. */
 int tf_geometry(int batch, int nx, int ny, int nz, int periodic, tf_geom* out);
 
+/* Per-plane counts of label 1 (uint64 [batch][nx]) and the largest label (int32, one) of a uint8
+ * label batch [batch][nx][ny][nz] in device memory, in one pass. Replaces the host-side 0/1 label
+ * check of Solver (taufactor.py:387-397) and the conductive fraction vol_x = mean(mask, (2, 3))
+ * (:42) for labels that serve as tf_pack phase indices as they are. TF_ERR_UNSUPPORTED if
+ * batch * nx > 65535. */
+int tf_label_stats(int batch, int nx, int ny, int nz, const uint8_t* labels_dev, uint64_t* plane_counts_dev,
+                   int32_t* max_label_dev, void* stream);
+
 /* Build the code buffer and the initial field from per-voxel phase indices.
  * Replaces ThroughTransportSolver.init_field + _pad (taufactor.py:282-291, :228-238),
  * Solver/PeriodicSolver/AnisotropicSolver.init_conductive_neighbours (:402-410, :493-499,

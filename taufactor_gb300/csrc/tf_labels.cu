@@ -1,0 +1,89 @@
+// Label statistics of a uint8 batch on the device (sm_103a): per-plane counts of label 1 and the
+// largest label, in one pass over the labels as the caller uploaded them. They replace the
+// host-side passes of Solver set-up: the 0/1 label check (taufactor/taufactor.py:387-397) and
+// the per-plane conductive fraction vol_x = mean(mask, (2, 3)) (taufactor.py:42).
+#include "tf_common.cuh"
+#include "tf_internal.h"
+
+namespace tf {
+
+// grid (chunks of a plane, batch * nx planes): each CTA counts the 1s in its chunk of plane
+// blockIdx.y with 16-byte loads (byte tail scalar), adds them to counts[plane] and raises
+// max_label.
+__global__ void __launch_bounds__(256) k_label_stats(const uint8_t* __restrict__ labels, long long plane_bytes,
+                                                      unsigned long long* __restrict__ counts,
+                                                      int32_t* __restrict__ max_label) {
+    const long long plane = blockIdx.y;
+    const uint8_t* base = labels + plane * plane_bytes;
+    // 16-byte groups of this plane (the plane may start unaligned: peel to the first boundary)
+    const long long mis = (long long)((16 - ((uintptr_t)base & 15)) & 15);
+    const long long head = mis < plane_bytes ? mis : plane_bytes;
+    const long long n16 = (plane_bytes - head) / 16;
+    const uint4* v = reinterpret_cast<const uint4*>(base + head);
+    unsigned int ones = 0;
+    uint32_t mxv = 0;  // per-byte running maximum
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n16; i += (long long)gridDim.x * blockDim.x) {
+        const uint4 q = v[i];
+        const uint32_t w[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            ones += __popc(__vcmpeq4(w[k], 0x01010101u)) >> 3;  // 0xff per byte equal to 1
+            mxv = __vmaxu4(mxv, w[k]);
+        }
+    }
+    unsigned int mx = max(max(mxv & 0xffu, (mxv >> 8) & 0xffu), max((mxv >> 16) & 0xffu, mxv >> 24));
+    // scalar head and tail bytes, by the first CTA of the plane
+    if (blockIdx.x == 0) {
+        const long long tail0 = head + n16 * 16;
+        for (long long i = threadIdx.x; i < head + (plane_bytes - tail0); i += blockDim.x) {
+            const long long j = i < head ? i : tail0 + (i - head);
+            const unsigned int b = base[j];
+            ones += b == 1u;
+            mx = max(mx, b);
+        }
+    }
+    for (int o = 16; o; o >>= 1) {
+        ones += __shfl_down_sync(0xffffffffu, ones, o);
+        mx = max(mx, __shfl_down_sync(0xffffffffu, mx, o));
+    }
+    __shared__ unsigned int s_ones[8], s_mx[8];
+    if ((threadIdx.x & 31) == 0) {
+        s_ones[threadIdx.x >> 5] = ones;
+        s_mx[threadIdx.x >> 5] = mx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned int t = 0, m = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+            t += s_ones[i];
+            m = max(m, s_mx[i]);
+        }
+        if (t) atomicAdd(&counts[plane], (unsigned long long)t);
+        atomicMax(max_label, (int)m);
+    }
+}
+
+}  // namespace tf
+
+using namespace tf;
+
+extern "C" int tf_label_stats(int batch, int nx, int ny, int nz, const uint8_t* labels_dev, uint64_t* plane_counts_dev,
+                              int32_t* max_label_dev, void* stream) {
+    if (batch < 1 || nx < 1 || ny < 1 || nz < 1 || !labels_dev || !plane_counts_dev || !max_label_dev)
+        return TF_ERR_ARG;
+    const long long planes = (long long)batch * nx;
+    if (planes > 65535) return TF_ERR_UNSUPPORTED;
+    cudaStream_t st = (cudaStream_t)stream;
+    const long long plane_bytes = (long long)ny * nz;
+    if (cudaMemsetAsync(plane_counts_dev, 0, sizeof(uint64_t) * planes, st) != cudaSuccess) return TF_ERR_CUDA;
+    if (cudaMemsetAsync(max_label_dev, 0, sizeof(int32_t), st) != cudaSuccess) return TF_ERR_CUDA;
+    // enough CTAs per plane to cover the machine a few times over, at most one per 4 KB
+    long long per_plane = (4LL * sm_count() * 8 + planes - 1) / planes;
+    const long long cap = (plane_bytes + 4095) / 4096;
+    if (per_plane > cap) per_plane = cap;
+    if (per_plane < 1) per_plane = 1;
+    k_label_stats<<<dim3((unsigned)per_plane, (unsigned)planes), 256, 0, st>>>(
+        labels_dev, plane_bytes, (unsigned long long*)plane_counts_dev, max_label_dev);
+    note_launch();
+    return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
+}

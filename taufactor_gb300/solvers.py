@@ -78,8 +78,12 @@ class SORSolver:
         if omega is None:
             omega = 2 - math.pi / (1.5 * self.Nx)  # taufactor.py:36-37
         self.omega = omega
-        phase, mask = self._phase_indices()
-        self.vol_x = plane_fraction(mask)
+        fast = self._device_labels()
+        if fast is not None:  # labels uploaded as they are; vol_x from one device pass
+            phase, self.vol_x = fast
+        else:
+            phase, mask = self._phase_indices()
+            self.vol_x = plane_fraction(mask)
         self._op = self._operator(float(omega))
         autotune.apply(self, *autotune.default_config(self))
         self._build(phase)
@@ -92,6 +96,11 @@ class SORSolver:
         self.walltime = 0.0
 
     # ------------------------------------------------------------------ hooks
+    def _device_labels(self):
+        """(phase indices already on the device, vol_x) when the labels can serve as phase
+        indices as they are, else None (then _phase_indices runs on the host)."""
+        return None
+
     def _phase_indices(self):
         """uint8 phase indices [B,X,Y,Z] for tf_pack and the bool conductive mask."""
         raise NotImplementedError
@@ -109,7 +118,8 @@ class SORSolver:
         return op
 
     # ------------------------------------------------------------------ device state
-    def _build(self, phase: np.ndarray):
+    def _build(self, phase):
+        """phase: uint8 [B,X,Y,Z] numpy array, or a uint8 tensor already on the device."""
         self._lib = _capi.load()
         g = TfGeom()
         check(self._lib.tf_geometry(self.batch_size, self.Nx, self.Ny, self.Nz, self._periodic, C.byref(g)),
@@ -122,7 +132,10 @@ class SORSolver:
             self._fb = torch.zeros(g.field_elems, dtype=torch.float32, device=dev)
             self._err = torch.zeros(1, dtype=torch.int32, device=dev)
             profile = self._initial_profile().to(dev)
-            phase_dev = torch.from_numpy(np.ascontiguousarray(phase, dtype=np.uint8)).to(dev)
+            if isinstance(phase, torch.Tensor):
+                phase_dev = phase
+            else:
+                phase_dev = torch.from_numpy(np.ascontiguousarray(phase, dtype=np.uint8)).to(dev)
             self._phase_dev, self._profile_dev = phase_dev, profile
             self._pack()
             self._flux_dev = torch.empty((self.batch_size, max(self.Nx - 1, 1)), dtype=torch.float64, device=dev)
@@ -462,7 +475,9 @@ class Solver(ThroughTransportSolver):
     """Two-phase solver: 1 = conductive, 0 = not (taufactor.py:355-419)."""
 
     def __init__(self, img, omega=None, D_0=1, device="cuda"):
-        self._check_binary_labels(img)
+        self._labels_checked = not self._labels_go_to_device(img, device)
+        if self._labels_checked:
+            self._check_binary_labels(img)
         self.conductive_labels = [1]
         super().__init__(img, omega=omega, device=device)
         self.D_0 = D_0
@@ -486,6 +501,47 @@ class Solver(ThroughTransportSolver):
                 "0 for non-conductive and 1 for conductive phase. "
                 f"Your image has the following labels: {u}. "
                 "If you have more than one conductive phase, use the multi-phase solver.")
+
+    @staticmethod
+    def _labels_go_to_device(img, device) -> bool:
+        """uint8 / bool labels on a usable CUDA device are checked there (tf_label_stats) rather
+        than by host passes; any other input keeps the reference's host check, which then also
+        comes before a device error as in the reference."""
+        if not isinstance(img, np.ndarray) or img.dtype not in (np.uint8, np.bool_) or not img.flags.c_contiguous:
+            return False
+        if img.ndim not in (2, 3, 4) or img.size == 0:
+            return False
+        try:
+            dev = torch.device(device)
+        except (RuntimeError, TypeError):
+            return False
+        planes = img.shape[0] * img.shape[1] if img.ndim == 4 else img.shape[0]
+        return dev.type == "cuda" and torch.cuda.is_available() and planes <= 65535
+
+    def _device_labels(self):
+        """The labels are the phase indices (1 = conductive): upload them as they are and take the
+        0/1 check and the per-plane conductive counts from one pass on the device."""
+        if self._labels_checked:
+            return None
+        lib = _capi.load()
+        B, X, Y, Z = self.cpu_img.shape
+        with torch.cuda.device(self.device):
+            labels = torch.from_numpy(self.cpu_img.view(np.uint8)).to(self.device)
+            counts = torch.empty((B, X), dtype=torch.int64, device=self.device)
+            top = torch.empty(1, dtype=torch.int32, device=self.device)
+            rc = lib.tf_label_stats(B, X, Y, Z, labels.data_ptr(), counts.data_ptr(), top.data_ptr(),
+                                    torch.cuda.current_stream(self.device).cuda_stream)
+            if rc == _capi.TF_ERR_UNSUPPORTED:
+                self._labels_checked = True
+                self._check_binary_labels(self.cpu_img)
+                return None
+            check(rc, "tf_label_stats")
+            counts_h = counts.cpu().numpy()
+            top_h = int(top.item())
+        self._labels_checked = True
+        if top_h > 1:
+            self._check_binary_labels(self.cpu_img)  # raises the reference's ValueError
+        return labels, counts_h / float(Y * Z)
 
     def _phase_indices(self):
         mask = self.cpu_img == 1

@@ -244,3 +244,27 @@ def test_device_spanning_test_long_path():
         assert bool(s.spans_x_device()[0]) == spans_x(v == 1)
     mp = tg.MultiPhaseSolver(np.where(img == 1, 2, 0).astype(np.uint8), {0: 0.0, 2: 0.7})
     assert bool(mp.spans_x_device()[0])
+
+
+def test_device_label_pass_matches_host_set_up():
+    """uint8 / bool labels are checked and counted on the device (tf_label_stats): vol_x equals
+    the host computation for ragged plane sizes (unaligned plane starts), the solve equals the
+    one set up from int64 labels (host path), and labels other than 0/1 raise the reference's
+    ValueError."""
+    from taufactor_gb300.solvers import plane_fraction
+
+    for shape, seed in (((2, 9, 7, 13), 31), ((1, 20, 33, 17), 32), ((3, 16, 16, 16), 33)):
+        img = random_binary(shape, seed)
+        a = tg.Solver(img)
+        assert np.array_equal(a.vol_x, plane_fraction(img == 1))
+        b = tg.Solver(img.astype(np.int64))  # host set-up
+        assert np.array_equal(a.vol_x, b.vol_x)
+        a.solve(verbose=False, conv_crit=1e-3)
+        b.solve(verbose=False, conv_crit=1e-3)
+        assert a.iter == b.iter and np.array_equal(a.D_eff, b.D_eff)
+        c = tg.Solver(img.astype(bool))
+        assert np.array_equal(c.vol_x, a.vol_x)
+    bad = random_binary((6, 6, 6), 34)
+    bad[3, 3, 3] = 2
+    with pytest.raises(ValueError, match="Input image must only contain 0s and 1s"):
+        tg.Solver(bad)
