@@ -1,7 +1,7 @@
 """GPU tests of the FP64 defect correction against the FP64 oracle (scipy CG to 1e-10).
 
 Tolerance: refined D_eff within 1e-8 relative of the oracle (both solve the same operator to a
-relative residual <= 1e-10); the spec bar is 1e-4.
+relative residual <= 1e-10); the accuracy bar of a converged solve is 1e-4.
 """
 import numpy as np
 import pytest
