@@ -68,6 +68,11 @@ def test_entry_points_reject_bad_arguments_without_launching(lib):
     assert lib.tf_layer_sums(C.byref(bad), C.byref(op), 16, 16, 16, 16, None) == _capi.TF_ERR_ARG
     op.kind = 7
     assert lib.tf_unpack(C.byref(g), C.byref(op), 16, 16, None) == _capi.TF_ERR_ARG
+    assert lib.tf_label_stats(0, 4, 4, 4, 16, 16, 16, None) == _capi.TF_ERR_ARG
+    assert lib.tf_label_stats(1, 4, 4, 4, None, 16, 16, None) == _capi.TF_ERR_ARG
+    assert lib.tf_label_stats(2, 40000, 4, 4, 16, 16, 16, None) == _capi.TF_ERR_UNSUPPORTED  # > 65535 planes
+    assert lib.tf_batch_advance_tile(16, 16, 4, 16, 0, 3, None) == _capi.TF_ERR_ARG  # no tile class 3
+    assert lib.tf_batch_advance_rhs_tile(16, 16, 4, 16, 0, -1, None) == _capi.TF_ERR_ARG
     assert lib.tf_launch_count() == n0
     with pytest.raises(ValueError):
         _capi.check(_capi.TF_ERR_ARG, "x")
