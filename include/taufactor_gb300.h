@@ -312,6 +312,18 @@ int tf_kappa_advance(const tf_geom* g, const tf_operator* op, float* field_dev, 
 int tf_spans_x(int batch, int nx, int ny, int nz, const uint8_t* phase_dev, const uint8_t* conductive,
                int32_t* labels_dev, int32_t* spans_dev, int32_t* err_dev, void* stream);
 
+/* Phase indices of the anchored system (no reference counterpart; the system the FP64 oracle
+ * solves): out_phase_dev[v] = phase_dev[v] where v belongs to a face-connected cluster of
+ * conductive voxels (conductive[phase] != 0, host table of 256 entries; wrapping in y / z for
+ * the TF_PERIODIC_* bits of `periodic`) that touches x = 0 or x = nx - 1, else 0. Clusters that
+ * touch neither face carry no flux; with a rounded float32 diagonal their block of the operator
+ * is nearly singular, and the FP64 refinement packs its codes from this map so that they stay out
+ * of its residual. labels_dev int32 and flags_dev uint8 are scratch of batch*nx*ny*nz entries;
+ * err_dev: TF_ERR_TIMEOUT if a bounded loop ran out. batch * nx * ny * nz must stay below 2^31. */
+int tf_anchored_phase(int batch, int nx, int ny, int nz, int periodic, const uint8_t* phase_dev,
+                      const uint8_t* conductive, int32_t* labels_dev, uint8_t* flags_dev, uint8_t* out_phase_dev,
+                      int32_t* err_dev, void* stream);
+
 /* The operator's faces for tf_kappa_advance_faces, computed once per kappa field (float32, the
  * values the sweeps use; taufactor.py:586-603 with a per-voxel diffusivity): fx_dev holds
  * batch * (nx + 1) planes of field_elems / (batch * nx) floats each (plane x + 1 = the face

@@ -210,13 +210,44 @@ class SORSolver:
         """
         n_inner = inner_half_sweeps or max(400, 2 * (self.iter or 200))
         with torch.cuda.device(self.device):
-            c64, hist = refine_field(self._lib, self._geom, self._op, self._cur, self._code, self._err,
+            code = self._code if self._kind == TF_KIND_BINARY else self._anchored_code()
+            c64, hist = refine_field(self._lib, self._geom, self._op, self._cur, code, self._err,
                                      self._stream(), self.batch_size, tol, max_outer, n_inner)
         self._field64 = c64
         self.residual_history = hist
         self.tau, _ = self.compute_metrics()
         self.tau = np.where(self.tau == 0, np.inf, self.tau)
         return hist
+
+    def _anchored_code(self) -> torch.Tensor:
+        """Codes of the system the FP64 refinement solves: conductive voxels of clusters that touch
+        neither x-face are frozen (tf_anchored_phase), as in the FP64 oracle. Such a cluster carries
+        no flux; under a float32 diagonal (the rounded sum of its faces) its block of the operator
+        is nearly singular, so the float32 correction sweeps cannot remove its share of the
+        residual and the refinement would stall near 1e-8. The binary kind's integer diagonal
+        keeps the block exactly singular, and it uses its own codes."""
+        cached = getattr(self, "_code_anchored", None)
+        if cached is not None:
+            return cached
+        n = self.batch_size * self.Nx * self.Ny * self.Nz
+        dev = self.device
+        labels = torch.empty(n, dtype=torch.int32, device=dev)
+        flags = torch.empty(n, dtype=torch.uint8, device=dev)
+        phase = torch.empty(n, dtype=torch.uint8, device=dev)
+        st = self._stream()
+        check(self._lib.tf_anchored_phase(self.batch_size, self.Nx, self.Ny, self.Nz, self._periodic,
+                                          _ptr(self._phase_dev), self._conductive_table(), _ptr(labels),
+                                          _ptr(flags), _ptr(phase), _ptr(self._err), st), "tf_anchored_phase")
+        del labels, flags
+        code = torch.empty_like(self._code)
+        scratch = torch.empty(self._geom.field_elems, dtype=torch.float32, device=dev)
+        check(self._lib.tf_pack(C.byref(self._geom), C.byref(self._op), _ptr(phase), _ptr(self._profile_dev),
+                                _ptr(code), _ptr(scratch), st), "tf_pack")
+        if int(self._err.item()):
+            self._err.zero_()
+            raise _capi.TfError(_capi.TF_ERR_TIMEOUT, "tf_anchored_phase (device)")
+        self._code_anchored = code
+        return code
 
     def _advance(self, n: int):
         """n half-sweeps (reference iterations) starting at colour iter % 2."""
@@ -250,6 +281,15 @@ class SORSolver:
                 check(self._lib.tf_layer_sums_f64(C.byref(self._geom), C.byref(self._op), _ptr(self._field64),
                                                   _ptr(self._code), _ptr(self._flux_dev), _ptr(self._csum_dev),
                                                   self._stream()), "tf_layer_sums_f64")
+                anchored = getattr(self, "_code_anchored", None)
+                if anchored is not None:
+                    # the flux of the system the refinement solved: clusters that touch neither
+                    # x-face carry none (their faces are left out, as in the FP64 oracle); the
+                    # field means keep every conductive voxel
+                    scratch = torch.empty_like(self._csum_dev)
+                    check(self._lib.tf_layer_sums_f64(C.byref(self._geom), C.byref(self._op), _ptr(self._field64),
+                                                      _ptr(anchored), _ptr(self._flux_dev), _ptr(scratch),
+                                                      self._stream()), "tf_layer_sums_f64")
             else:
                 check(self._lib.tf_layer_sums(C.byref(self._geom), C.byref(self._op), _ptr(self._cur),
                                               _ptr(self._code), _ptr(self._flux_dev), _ptr(self._csum_dev),

@@ -68,6 +68,8 @@ def test_entry_points_reject_bad_arguments_without_launching(lib):
     assert lib.tf_layer_sums(C.byref(bad), C.byref(op), 16, 16, 16, 16, None) == _capi.TF_ERR_ARG
     op.kind = 7
     assert lib.tf_unpack(C.byref(g), C.byref(op), 16, 16, None) == _capi.TF_ERR_ARG
+    assert lib.tf_anchored_phase(1, 4, 4, 4, 0, None, 16, 16, 16, 16, 16, None) == _capi.TF_ERR_ARG
+    assert lib.tf_anchored_phase(1, 0, 4, 4, 0, 16, 16, 16, 16, 16, 16, None) == _capi.TF_ERR_ARG
     assert lib.tf_label_stats(0, 4, 4, 4, 16, 16, 16, None) == _capi.TF_ERR_ARG
     assert lib.tf_label_stats(1, 4, 4, 4, None, 16, 16, None) == _capi.TF_ERR_ARG
     assert lib.tf_label_stats(2, 40000, 4, 4, 16, 16, 16, None) == _capi.TF_ERR_UNSUPPORTED  # > 65535 planes

@@ -104,3 +104,45 @@ def test_rhs_half_sweeps_bitwise(kind, shape, kw):
               "tf_unpack")
         got = out.cpu().numpy()[:, :, 1:-1, 1:-1]
         assert np.array_equal(got, o.field[:, :, 1:-1, 1:-1]), n
+
+
+def _pocket_volume():
+    """Three labels (blurred, seed 48) with a conductive pocket sealed inside a shell of the
+    zero-conductivity label: a cluster that touches neither x-face."""
+    from cases import _blur_labels
+
+    img = _blur_labels((30, 24, 28), 48)
+    img[10:20, 8:16, 8:16] = 0
+    img[12:18, 10:14, 10:14] = 1
+    return img
+
+
+def _wrap_path_volume():
+    """Label 1 channels in label 0 (conductivity 0): the only path from x = 0 to x = nx - 1 runs
+    through a middle segment that touches the others across the periodic y face alone."""
+    img = np.zeros((24, 12, 10), dtype=np.uint8)
+    img[:9, 0:2, 3:6] = 1      # touches x = 0
+    img[7:17, 10:12, 3:6] = 1  # middle segment: rows 10-11 wrap onto rows 0-1
+    img[15:, 0:2, 3:6] = 1     # touches x = nx - 1
+    return img
+
+
+@pytest.mark.parametrize("kind,make,ds", [
+    ("multiphase", _pocket_volume, {0: 0.0, 1: 1.0, 2: 0.1}),
+    ("periodic_multiphase", _pocket_volume, {0: 0.0, 1: 1.0, 2: 0.1}),
+    ("periodic_multiphase", _wrap_path_volume, {0: 0.0, 1: 1.0}),
+    ("anisotropic", lambda: (_pocket_volume() > 0).astype(np.uint8), None),
+])
+def test_refinement_with_unanchored_clusters_reaches_tight_tolerance(kind, make, ds):
+    """With float32 faces the diagonal is a rounded sum, so the block of a cluster touching
+    neither x-face is nearly singular; the refinement solves the anchored system (as the FP64
+    oracle does) and reaches 1e-12, and clusters joined across a periodic face stay in it."""
+    img = make()
+    kw = {"spacing": (1.0, 1.3, 0.7)} if kind == "anisotropic" else {"diffusivities": ds}
+    s = _solver(kind, img, kw)
+    s.solve(verbose=False, conv_crit=1e-3)
+    hist = s.refine(tol=1e-12, max_outer=20)
+    assert hist[-1] < 1e-12, hist
+    o = OracleSolve(img, kind=kind, **kw)
+    d64, _, _ = d_eff_fp64(o, rtol=1e-12)
+    np.testing.assert_allclose(s.D_eff, d64, rtol=1e-9, atol=1e-14)
