@@ -57,7 +57,8 @@ def build(verbose_ptxas: bool = False, force: bool = False) -> str:
             and os.path.getmtime(lib) >= max(os.path.getmtime(d) for d in deps)):
         return lib
     nvcc = nvcc_path()
-    with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+    # one compiler process per translation unit, up to the host's cores (16 on the GPU machines)
+    with cf.ThreadPoolExecutor(max_workers=max(1, min(os.cpu_count() or 8, 16, len(srcs)))) as ex:
         results = list(ex.map(lambda s: _compile(nvcc, s, verbose_ptxas), srcs))
     if verbose_ptxas:
         for _, log in results:
