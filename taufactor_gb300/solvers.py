@@ -198,7 +198,8 @@ class SORSolver:
         """Pick the fastest tile shape / half-sweeps per launch for these volumes (results unchanged)."""
         return autotune.tune(self, half_sweeps)
 
-    def refine(self, tol: float = 1e-10, max_outer: int = 12, inner_half_sweeps: int | None = None):
+    def refine(self, tol: float = 1e-10, max_outer: int = 12, inner_half_sweeps: int | None = None,
+               omega: float | None = None):
         """FP64 defect correction of the current field; returns the relative residual history.
 
         Keeps the solution in float64, forms r = b - A c in float64 on the device, solves A e = r
@@ -206,13 +207,15 @@ class SORSolver:
         adds e in float64, until max over volumes of ||r|| / ||b|| < tol. The reference has no
         such step (it iterates in float32 only, taufactor.py:172-182). Afterwards the metrics
         (D_eff, tau, flux_1d, c_x, tau_x) come from the float64 field and the float32 field holds
-        its rounding.
+        its rounding. omega: over-relaxation of the correction sweeps (default: the solve's own;
+        2 - 3/Nx needed 9 instead of 13 outer steps on a 256^3 binary volume and 14 instead of 15
+        on a 320^3 three-label one).
         """
         n_inner = inner_half_sweeps or max(400, 2 * (self.iter or 200))
         with torch.cuda.device(self.device):
             code = self._code if self._kind == TF_KIND_BINARY else self._anchored_code()
             c64, hist = refine_field(self._lib, self._geom, self._op, self._cur, code, self._err,
-                                     self._stream(), self.batch_size, tol, max_outer, n_inner)
+                                     self._stream(), self.batch_size, tol, max_outer, n_inner, omega)
         self._field64 = c64
         self.residual_history = hist
         self.tau, _ = self.compute_metrics()
@@ -427,12 +430,15 @@ class SORSolver:
 
 
 def refine_field(lib, g: TfGeom, op: TfOperator, cur: torch.Tensor, code: torch.Tensor, err: torch.Tensor, stream,
-                 batch: int, tol: float, max_outer: int, n_inner: int):
+                 batch: int, tol: float, max_outer: int, n_inner: int, omega: float | None = None):
     """FP64 defect correction of the float32 field `cur` (updated in place with the rounding of
-    the result); returns the float64 field and the max-over-volumes relative residual history."""
+    the result); returns the float64 field and the max-over-volumes relative residual history.
+    omega: over-relaxation of the correction sweeps (default: the solve's own)."""
     gp = C.byref(g)
     op0 = TfOperator.from_buffer_copy(op)
     op0.ghost_lo = op0.ghost_hi = 0.0
+    if omega is not None:
+        op0.omega = float(F32(omega))
     dev = cur.device
     c64 = torch.empty(g.field_elems, dtype=torch.float64, device=dev)
     check(lib.tf_widen_f64(gp, _ptr(cur), _ptr(c64), stream), "tf_widen_f64")

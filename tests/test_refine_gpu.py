@@ -146,3 +146,17 @@ def test_refinement_with_unanchored_clusters_reaches_tight_tolerance(kind, make,
     o = OracleSolve(img, kind=kind, **kw)
     d64, _, _ = d_eff_fp64(o, rtol=1e-12)
     np.testing.assert_allclose(s.D_eff, d64, rtol=1e-9, atol=1e-14)
+
+
+def test_refinement_with_its_own_omega_reaches_the_same_solution():
+    """The correction sweeps may over-relax with their own omega (no reference counterpart): the
+    refined system and its D_eff do not change, only the rate."""
+    img = random_binary((40, 32, 36), 53, 0.6)
+    a = tg.Solver(img)
+    a.solve(verbose=False, conv_crit=1e-3)
+    ha = a.refine(tol=1e-12, max_outer=30)
+    b = tg.Solver(img)
+    b.solve(verbose=False, conv_crit=1e-3)
+    hb = b.refine(tol=1e-12, max_outer=30, omega=2 - 3 / img.shape[0])
+    assert ha[-1] < 1e-12 and hb[-1] < 1e-12
+    np.testing.assert_allclose(b.D_eff, a.D_eff, rtol=1e-11, atol=0)
