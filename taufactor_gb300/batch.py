@@ -36,7 +36,7 @@ from . import _capi
 from ._capi import (TF_BATCH_ACTIVE, TF_BATCH_CONVERGED, TF_BATCH_NEEDS_HOST, TF_KIND_BINARY, TF_PERIODIC_Y,
                     TF_PERIODIC_Z, TfBatchState, TfGeom, TfOperator, check)
 from .percolation import spans_x
-from .solvers import layer_metrics
+from .solvers import layer_metrics, unique_labels
 
 INTERVAL = 100  # half-sweeps between convergence checks (taufactor.py:184-185)
 CHUNK = 32  # planes per work item of the batched sweep
@@ -107,7 +107,7 @@ class BatchSolve:
             for v, img in enumerate(vols):
                 if img.ndim != 3:
                     raise ValueError("every volume must be 3-D")
-                u = np.unique(img)
+                u = unique_labels(img)
                 if len(u) > 2 or u.max() not in (0, 1) or u.min() not in (0, 1):
                     raise ValueError(f"volume {v}: labels must be 0/1, got {u}")
                 res = VolumeResult(img, per[v])
