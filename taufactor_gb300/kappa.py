@@ -32,7 +32,7 @@ import torch
 
 from . import _capi
 from ._capi import TF_KIND_MULTIPHASE, TF_PERIODIC_Y, TF_PERIODIC_Z, TfGeom, TfOperator, check
-from .solvers import layer_metrics
+from .solvers import layer_metrics, relative_residual
 
 
 def _ptr(t: torch.Tensor) -> int:
@@ -194,7 +194,7 @@ class KappaSolver:
             check(lib.tf_kappa_residual_f64(C.byref(g), C.byref(self._op), _ptr(x64), _ptr(self._ks),
                                             _ptr(b64) if b64 is not None else None, self._coeff64, _ptr(rhs),
                                             _ptr(r2), _ptr(b2), st), "tf_kappa_residual_f64")
-            rel = float((torch.sqrt(r2.sum(dim=1)) / torch.sqrt(b2.sum(dim=1)).clamp_min(1e-300)).max().item())
+            rel = relative_residual(r2, b2)
             hist.append(rel)
             if rel < tol or outer == max_outer:
                 break

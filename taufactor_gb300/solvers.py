@@ -429,6 +429,15 @@ class SORSolver:
                   f"{torch.cuda.max_memory_reserved(device=self.device) / 1e6:.2f} MB reserved)")
 
 
+def relative_residual(r2: torch.Tensor, b2: torch.Tensor) -> float:
+    """max over volumes of ||r|| / ||b|| from the per-plane float64 sums of r^2 and b^2 ([B, Nx],
+    device), reduced on the host: the sums are a few KB, and the host keeps torch's reduction
+    kernels (slow to load on first use) out of the solve path."""
+    r = r2.cpu().numpy().sum(axis=1)
+    b = b2.cpu().numpy().sum(axis=1)
+    return float((np.sqrt(r) / np.maximum(np.sqrt(b), 1e-300)).max())
+
+
 def refine_field(lib, g: TfGeom, op: TfOperator, cur: torch.Tensor, code: torch.Tensor, err: torch.Tensor, stream,
                  batch: int, tol: float, max_outer: int, n_inner: int, omega: float | None = None):
     """FP64 defect correction of the float32 field `cur` (updated in place with the rounding of
@@ -451,8 +460,7 @@ def refine_field(lib, g: TfGeom, op: TfOperator, cur: torch.Tensor, code: torch.
     for outer in range(max_outer + 1):
         check(lib.tf_residual_f64(gp, C.byref(op), _ptr(c64), _ptr(code), _ptr(rhs), _ptr(r2), _ptr(b2), stream),
               "tf_residual_f64")
-        bn = torch.sqrt(b2.sum(dim=1)).clamp_min(1e-300)
-        rel = float((torch.sqrt(r2.sum(dim=1)) / bn).max().item())
+        rel = relative_residual(r2, b2)
         hist.append(rel)
         if rel < tol or outer == max_outer:
             break
