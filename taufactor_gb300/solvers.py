@@ -742,18 +742,20 @@ class MultiPhaseSolver(ThroughTransportSolver):
         """
         from .kappa import KappaSolver
 
-        lab = torch.from_numpy(np.ascontiguousarray(self.cpu_img)).to(self.device)
-        kap = torch.zeros(lab.shape, dtype=torch.float32, device=self.device)
-        for p in unique_labels(self.cpu_img):
-            kap[lab == p] = float(F32(self.Ds.get(int(p), 0.0)))
+        # kappa = D[label] and the per-label sums of the gradient on the host (a lookup table and
+        # a bincount over the labels), so no torch reduction or mask kernels join the GPU path
+        labels = unique_labels(self.cpu_img)
+        img = np.asarray(self.cpu_img)
+        idx = np.searchsorted(labels, img)  # label -> position in `labels`
+        lut = np.array([F32(self.Ds.get(int(p), 0.0)) for p in labels], dtype=np.float32)
+        kap = torch.from_numpy(np.ascontiguousarray(lut[idx])).to(self.device)
         ks = KappaSolver(kap, periodic=bool(self._periodic), omega=self.omega, D_0=self.D_0, device=self.device)
         ks.solve(conv_crit=conv_crit, refine={"tol": tol})
-        g = ks.gradient(tol=tol)
+        g = ks.gradient(tol=tol).cpu().numpy()
         self.kappa_solver = ks
-        out = {}
-        for p in unique_labels(self.cpu_img):
-            out[int(p)] = (g * (lab == p)).sum(dim=(1, 2, 3)).cpu().numpy()
-        return out
+        sums = np.stack([np.bincount(idx[b].ravel(), weights=g[b].ravel(), minlength=len(labels))
+                         for b in range(g.shape[0])])
+        return {int(p): sums[:, i] for i, p in enumerate(labels)}
 
 
 class PeriodicMultiPhaseSolver(MultiPhaseSolver):
