@@ -96,6 +96,13 @@ int tf_geometry(int batch, int nx, int ny, int nz, int periodic, tf_geom* out);
 int tf_label_stats(int batch, int nx, int ny, int nz, const uint8_t* labels_dev, uint64_t* plane_counts_dev,
                    int32_t* max_label_dev, void* stream);
 
+/* Per-plane count of kappa > 0 (uint64 [batch][nx]) and float64 sum of kappa ([batch][nx]) of a
+ * float32 conductivity field [batch][nx][ny][nz] in device memory, and *bad_dev = 1 if any value
+ * is negative, infinite or NaN (else 0). One CTA per plane, fixed summation order. KappaSolver
+ * set-up: vol_x, D_mean and the input check without torch reductions. */
+int tf_kappa_stats(int batch, int nx, int ny, int nz, const float* kappa_dev, uint64_t* plane_positive_dev,
+                   double* plane_sums_dev, int32_t* bad_dev, void* stream);
+
 /* Build the code buffer and the initial field from per-voxel phase indices.
  * Replaces ThroughTransportSolver.init_field + _pad (taufactor.py:282-291, :228-238),
  * Solver/PeriodicSolver/AnisotropicSolver.init_conductive_neighbours (:402-410, :493-499,

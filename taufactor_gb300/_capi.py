@@ -29,6 +29,7 @@ EXPORTS = (
     "tf_kappa_faces", "tf_kappa_advance_faces", "tf_spans_x",
     "tf_impedance_pack", "tf_impedance_fill", "tf_impedance_sweep", "tf_impedance_metrics",
     "tf_batch_advance_tile", "tf_batch_advance_rhs_tile", "tf_label_stats", "tf_anchored_phase",
+    "tf_kappa_stats",
 )
 TF_IMP_TABLE = 56
 TF_BATCH_ACTIVE, TF_BATCH_CONVERGED, TF_BATCH_NEEDS_HOST = 0, 1, 2
@@ -106,6 +107,7 @@ def load():
         "tf_batch_advance_rhs": (i32, [vp, vp, i32, vp, i32, vp]),
         "tf_batch_advance_tile": (i32, [vp, vp, i32, vp, i32, i32, vp]),
         "tf_label_stats": (i32, [i32, i32, i32, i32, vp, vp, vp, vp]),
+        "tf_kappa_stats": (i32, [i32, i32, i32, i32, vp, vp, vp, vp, vp]),
         "tf_anchored_phase": (i32, [i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp, vp]),
         "tf_batch_advance_rhs_tile": (i32, [vp, vp, i32, vp, i32, i32, vp]),
         "tf_batch_layer_sums": (i32, [vp, vp, i32, vp, i32, vp, vp, vp]),

@@ -1,7 +1,8 @@
-// Label statistics of a uint8 batch on the device (sm_103a): per-plane counts of label 1 and the
-// largest label, in one pass over the labels as the caller uploaded them. They replace the
-// host-side passes of Solver set-up: the 0/1 label check (taufactor/taufactor.py:387-397) and
-// the per-plane conductive fraction vol_x = mean(mask, (2, 3)) (taufactor.py:42).
+// Set-up statistics on the device (sm_103a), one pass over the input as the caller uploaded it:
+// for uint8 labels the per-plane counts of label 1 and the largest label (Solver set-up: the 0/1
+// label check, taufactor/taufactor.py:387-397, and vol_x = mean(mask, (2, 3)), :42); for a
+// per-voxel conductivity the per-plane count of kappa > 0, the per-plane float64 sum and a
+// validity flag (KappaSolver set-up).
 #include "tf_common.cuh"
 #include "tf_internal.h"
 
@@ -84,6 +85,70 @@ extern "C" int tf_label_stats(int batch, int nx, int ny, int nz, const uint8_t* 
     if (per_plane < 1) per_plane = 1;
     k_label_stats<<<dim3((unsigned)per_plane, (unsigned)planes), 256, 0, st>>>(
         labels_dev, plane_bytes, (unsigned long long*)plane_counts_dev, max_label_dev);
+    note_launch();
+    return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
+}
+
+// Per-voxel conductivity statistics (KappaSolver set-up): per plane the count of kappa > 0 and the
+// float64 sum of kappa, and a flag for any value that is negative, infinite or NaN. One CTA per
+// plane with a fixed-order reduction, so the sums do not depend on scheduling.
+namespace tf {
+
+__global__ void __launch_bounds__(256) k_kappa_stats(const float* __restrict__ kappa, long long plane_elems,
+                                                      unsigned long long* __restrict__ positive,
+                                                      double* __restrict__ sums, int32_t* __restrict__ bad) {
+    const long long plane = blockIdx.x;
+    const float* base = kappa + plane * plane_elems;
+    unsigned int npos = 0;
+    double s = 0.0;
+    int badf = 0;
+    for (long long i = threadIdx.x; i < plane_elems; i += blockDim.x) {
+        const float k = base[i];
+        badf |= !(k >= 0.0f) || isinf(k);
+        npos += k > 0.0f;
+        s += (double)k;
+    }
+    for (int o = 16; o; o >>= 1) {
+        npos += __shfl_down_sync(0xffffffffu, npos, o);
+        s += __shfl_down_sync(0xffffffffu, s, o);
+        badf |= __shfl_down_sync(0xffffffffu, badf, o);
+    }
+    __shared__ unsigned int s_pos[8];
+    __shared__ double s_sum[8];
+    __shared__ int s_bad[8];
+    if ((threadIdx.x & 31) == 0) {
+        s_pos[threadIdx.x >> 5] = npos;
+        s_sum[threadIdx.x >> 5] = s;
+        s_bad[threadIdx.x >> 5] = badf;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        unsigned long long p = 0;
+        double t = 0.0;
+        int b = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); ++i) {
+            p += s_pos[i];
+            t += s_sum[i];
+            b |= s_bad[i];
+        }
+        positive[plane] = p;
+        sums[plane] = t;
+        if (b) atomicOr(bad, 1);
+    }
+}
+
+}  // namespace tf
+
+extern "C" int tf_kappa_stats(int batch, int nx, int ny, int nz, const float* kappa_dev, uint64_t* plane_positive_dev,
+                              double* plane_sums_dev, int32_t* bad_dev, void* stream) {
+    if (batch < 1 || nx < 1 || ny < 1 || nz < 1 || !kappa_dev || !plane_positive_dev || !plane_sums_dev || !bad_dev)
+        return TF_ERR_ARG;
+    const long long planes = (long long)batch * nx;
+    if (planes > 0x7fffffffLL) return TF_ERR_UNSUPPORTED;
+    cudaStream_t st = (cudaStream_t)stream;
+    if (cudaMemsetAsync(bad_dev, 0, sizeof(int32_t), st) != cudaSuccess) return TF_ERR_CUDA;
+    k_kappa_stats<<<(unsigned)planes, 256, 0, st>>>(kappa_dev, (long long)ny * nz,
+                                                   (unsigned long long*)plane_positive_dev, plane_sums_dev, bad_dev);
     note_launch();
     return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
 }

@@ -65,8 +65,6 @@ class KappaSolver:
             k = k[None]
         if k.dim() != 4:
             raise ValueError("kappa must be [X,Y,Z] or [B,X,Y,Z]")
-        if not torch.isfinite(k).all() or (k < 0).any():
-            raise ValueError("kappa must be finite and >= 0")
         self.batch_size, self.Nx, self.Ny, self.Nz = k.shape
         if self.Nx < 2:
             raise ValueError("need at least two planes along x")
@@ -74,13 +72,22 @@ class KappaSolver:
         self.periodic = bool(periodic)
         self.omega = 2 - math.pi / (1.5 * self.Nx) if omega is None else omega
         self.D_0 = D_0
-        kc = self.kappa.double()
-        mask = kc > 0
-        self.vol_x = mask.double().mean(dim=(2, 3)).cpu().numpy()
-        self.D_mean = kc.mean(dim=(1, 2, 3)).cpu().numpy()
+        self._lib = lib = _capi.load()
+        # input check, vol_x and D_mean from one device pass (tf_kappa_stats): no torch reductions
+        B, X, Y, Z = k.shape
+        with torch.cuda.device(self.device):
+            pos = torch.empty((B, X), dtype=torch.int64, device=self.device)
+            sums = torch.empty((B, X), dtype=torch.float64, device=self.device)
+            bad = torch.empty(1, dtype=torch.int32, device=self.device)
+            check(lib.tf_kappa_stats(B, X, Y, Z, _ptr(self.kappa), _ptr(pos), _ptr(sums), _ptr(bad), self._stream()),
+                  "tf_kappa_stats")
+            pos_h, sums_h, bad_h = pos.cpu().numpy(), sums.cpu().numpy(), int(bad.item())
+        if bad_h:
+            raise ValueError("kappa must be finite and >= 0")
+        self.vol_x = pos_h / float(Y * Z)
+        self.D_mean = sums_h.sum(axis=1) / float(X * Y * Z)
         self.cpu_img = None  # built lazily for the percolation fallback
         self.conductive_labels = [1]
-        self._lib = lib = _capi.load()
         g = self._geom = TfGeom()
         pflag = (TF_PERIODIC_Y | TF_PERIODIC_Z) if self.periodic else 0
         check(lib.tf_geometry(self.batch_size, self.Nx, self.Ny, self.Nz, pflag, C.byref(g)), "tf_geometry")

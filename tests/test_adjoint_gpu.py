@@ -152,3 +152,21 @@ def test_multiphase_phase_gradients_match_finite_differences():
         hp = float(np.float32(up[p])) - float(np.float32(dn[p]))
         fd = (a.D_eff[0] - b.D_eff[0]) / hp
         assert abs(fd - grads[p][0]) / abs(fd) < 1e-3, (p, fd, grads[p][0])
+
+
+def test_kappa_set_up_statistics_and_input_check():
+    """vol_x and D_mean come from one device pass (tf_kappa_stats) and match the host
+    computation; negative, infinite and NaN conductivities are refused."""
+    import taufactor_gb300 as tg
+
+    rng = np.random.default_rng(61)
+    k = rng.random((2, 9, 11, 13)).astype(np.float32)
+    k[k < 0.3] = 0.0
+    s = tg.KappaSolver(k)
+    assert np.array_equal(s.vol_x, (k > 0).reshape(2, 9, -1).sum(axis=2) / float(11 * 13))
+    np.testing.assert_allclose(s.D_mean, k.astype(np.float64).mean(axis=(1, 2, 3)), rtol=1e-14, atol=0)
+    for v in (-0.5, np.inf, np.nan):
+        bad = k.copy()
+        bad[1, 4, 5, 6] = v
+        with pytest.raises(ValueError, match="finite and >= 0"):
+            tg.KappaSolver(bad)
