@@ -68,7 +68,8 @@ typedef struct tf_operator {
     float ghost_lo, ghost_hi;  /* Dirichlet ghost values 2*bc: -1 (x = -1) and +1 (x = nx)     */
     float ky, kz;              /* anisotropic y, z weights (dx/dy)^2, (dx/dz)^2                */
     int32_t n_phases;          /* multiphase: phases 1..n_phases                               */
-    int32_t tile;              /* tiled-kernel tile shape: 0 = 16x64, 1 = 16x128, 2 = 32x64    */
+    int32_t tile;              /* tiled-kernel tile shape: 0 = 16x64, 1 = 16x128, 2 = 32x64,   */
+                               /* 3 = 16x128 row pairs (binary; even half-sweeps per launch)    */
     int32_t k_max;             /* half-sweeps per tiled launch, 1..4 (0 = 4)                   */
     float divisor[256];        /* binary/anisotropic: code -> diagonal (inf = frozen voxel)    */
     float face[32 * 32];       /* multiphase: [phase a][phase b] harmonic face conductance     */
@@ -284,10 +285,14 @@ int tf_batch_tick(int32_t* iter_base_dev, int half_sweeps, void* stream);
  * per-layer sums themselves are not returned. No counterpart in the reference.
  *   Limit: flux_len and csum_len (the arena lengths the descriptor's offsets were built for:
  *   sum of nx-1, resp. nx, over the volumes) must each be <= 65536, else TF_ERR_UNSUPPORTED.
+ *   desc_dev must be a table that tf_batch_describe built on the current device, with n_vol at
+ *   most its volumes and every offset it was given ending within flux_len / csum_len; anything
+ *   else is TF_ERR_ARG, before any launch. Plane items outside the table's volumes are skipped.
  *   Allocates nothing (no cudaMalloc/cudaFree). The first call on a device looks up the device
- *   address of the static array for that device (make it before any stream capture); the
- *   array is shared by every call in the process and keeps the last call's contents, so calls
- *   whose work overlaps on the GPU race. It holds 1 MiB on every GPU that loads the library. */
+ *   address of the static array for that device (make it before any stream capture), and looks
+ *   it up again if the device's context has changed since (cudaDeviceReset); the array is shared
+ *   by every call in the process and keeps the last call's contents, so calls whose work
+ *   overlaps on the GPU race. It holds 1 MiB on every GPU that loads the library. */
 int tf_batch_converge_static(const void* desc_dev, const int32_t* planes_dev, int n_planes, int n_vol,
                              int64_t flux_len, int64_t csum_len, tf_batch_state state, double conv_crit,
                              int interval, int cur_in_b, void* stream);

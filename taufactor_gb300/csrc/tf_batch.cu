@@ -20,7 +20,9 @@
 // volume): k_stream_multi_rhs runs every volume's inner half-sweeps in the same launches, each
 // volume for its own number of launches.
 #include <cstring>
+#include <map>
 #include <mutex>
+#include <utility>
 #include <vector>
 
 #include "tf_layers.cuh"
@@ -85,15 +87,22 @@ __global__ void __launch_bounds__(StreamShape<TY, TZ, BK>::NT, StreamShape<TY, T
 // One CTA per (volume, plane): float64 sums of the masked x-flux through face x|x+1 and of the
 // field in plane x (taufactor.py:294-296, :307, :412-419), exactly as the single-volume
 // k_layer_sums sums them. Binary operators only.
+// GUARDED (the static-scratch path): items naming a volume >= n_desc or a plane outside the
+// volume are skipped, and so is any sum whose index would reach past flux_cap / csum_cap.
+template <bool GUARDED>
 __global__ void __launch_bounds__(256) k_layer_sums_multi(const VolDesc* __restrict__ desc,
                                                           const int2* __restrict__ planes,
                                                           const int32_t* __restrict__ status, int cur_in_b,
-                                                          double* __restrict__ flux, double* __restrict__ csum) {
+                                                          double* __restrict__ flux, double* __restrict__ csum,
+                                                          int n_desc = 0, long long flux_cap = 0,
+                                                          long long csum_cap = 0) {
     const int2 item = planes[blockIdx.x];
     const int v = item.x, x = item.y;
+    if (GUARDED && (v < 0 || v >= n_desc)) return;
     if (status[v] != TF_BATCH_ACTIVE) return;
     const VolDesc* d = desc + v;
     const Geo g = d->ab.g;
+    if (GUARDED && (x < 0 || x >= g.NX)) return;
     const float* field = cur_in_b ? d->ab.out : d->ba.out;  // ab.out is buffer B
     const bool has_flux = x + 1 < g.NX;
     double fs = 0.0, cs = 0.0;
@@ -101,8 +110,9 @@ __global__ void __launch_bounds__(256) k_layer_sums_multi(const VolDesc* __restr
                                    nullptr, fs, cs);
     block_sum_pair(fs, cs);
     if (threadIdx.x == 0) {
-        if (has_flux) flux[d->flux_off + x] = fs;
-        csum[d->csum_off + x] = cs;
+        const long long fi = d->flux_off + x, ci = d->csum_off + x;
+        if (has_flux && (!GUARDED || (fi >= 0 && fi < flux_cap))) flux[fi] = fs;
+        if (!GUARDED || (ci >= 0 && ci < csum_cap)) csum[ci] = cs;
     }
 }
 
@@ -184,6 +194,34 @@ void tf_batch_tile(int* tile_y, int* tile_z, int* half_sweeps) {
 
 namespace tf {
 
+// What tf_batch_describe built at a descriptor address (per device): the number of volumes and
+// the end of the layer-sum offsets, max over v of flux_off + nx - 1 and csum_off + nx (-1 for a
+// correction-solve table, which has no layer sums). tf_batch_converge_static checks its
+// arguments against it before writing sums into its fixed array.
+struct DescExtent {
+    int n_vol;
+    long long flux_end, csum_end;
+};
+static std::mutex g_extent_mu;
+static std::map<std::pair<int, const void*>, DescExtent> g_extent;
+
+static void record_extent(const void* desc_dev, const DescExtent& e) {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return;
+    std::lock_guard<std::mutex> lock(g_extent_mu);
+    g_extent[{dev, desc_dev}] = e;
+}
+
+static bool find_extent(const void* desc_dev, DescExtent* e) {
+    int dev = -1;
+    if (cudaGetDevice(&dev) != cudaSuccess) return false;
+    std::lock_guard<std::mutex> lock(g_extent_mu);
+    const auto it = g_extent.find({dev, desc_dev});
+    if (it == g_extent.end()) return false;
+    *e = it->second;
+    return true;
+}
+
 // Descriptor table of the plain solve (rhs == nullptr) or of the correction solve (rhs[v] = the
 // float32 right-hand side of volume v; Dirichlet ghosts 0; layer-sum fields unused).
 static int describe(int n_vol, const tf_geom* geoms, const tf_operator* ops, float* const* field_a,
@@ -191,10 +229,17 @@ static int describe(int n_vol, const tf_geom* geoms, const tf_operator* ops, flo
                     const int64_t* flux_off, const int64_t* csum_off, const double* d_mean, int32_t* err_dev,
                     void* desc_dev) {
     std::vector<VolDesc> h(n_vol);
+    DescExtent ext{n_vol, rhs ? -1 : 0, rhs ? -1 : 0};
     for (int v = 0; v < n_vol; ++v) {
         const tf_geom& gg = geoms[v];
         tf_operator op = ops[v];
         if (gg.batch != 1 || !gg.tiled || op.kind != TF_KIND_BINARY) return TF_ERR_UNSUPPORTED;
+        if ((flux_off && flux_off[v] < 0) || (csum_off && csum_off[v] < 0)) return TF_ERR_ARG;
+        if (!rhs) {
+            const long long fe = (flux_off ? flux_off[v] : 0) + gg.nx - 1, ce = (csum_off ? csum_off[v] : 0) + gg.nx;
+            ext.flux_end = fe > ext.flux_end ? fe : ext.flux_end;
+            ext.csum_end = ce > ext.csum_end ? ce : ext.csum_end;
+        }
         if (rhs && (!rhs[v] || (reinterpret_cast<uintptr_t>(rhs[v]) & 15))) return TF_ERR_ARG;
         if (rhs) op.ghost_lo = op.ghost_hi = 0.0f;
         VolDesc& d = h[v];
@@ -239,9 +284,10 @@ static int describe(int n_vol, const tf_geom* geoms, const tf_operator* ops, flo
                                   cudaSuccess &&
                               cudaFuncSetAttribute(k_stream_multi<BTY2, BTZ>, smem_attr, BShape2::SMEM) == cudaSuccess;
     if (!ok) return TF_ERR_CUDA;
-    return cudaMemcpy(desc_dev, h.data(), sizeof(VolDesc) * n_vol, cudaMemcpyHostToDevice) == cudaSuccess
-               ? TF_OK
-               : TF_ERR_CUDA;
+    if (cudaMemcpy(desc_dev, h.data(), sizeof(VolDesc) * n_vol, cudaMemcpyHostToDevice) != cudaSuccess)
+        return TF_ERR_CUDA;
+    record_extent(desc_dev, ext);
+    return TF_OK;
 }
 
 }  // namespace tf
@@ -311,7 +357,7 @@ int tf_batch_advance(const void* desc_dev, const int32_t* work_dev, int n_work, 
 int tf_batch_layer_sums(const void* desc_dev, const int32_t* planes_dev, int n_planes, const int32_t* status_dev,
                         int cur_in_b, double* flux_dev, double* csum_dev, void* stream) {
     if (!desc_dev || !planes_dev || n_planes <= 0 || !status_dev || !flux_dev || !csum_dev) return TF_ERR_ARG;
-    k_layer_sums_multi<<<n_planes, 256, 0, (cudaStream_t)stream>>>(static_cast<const VolDesc*>(desc_dev),
+    k_layer_sums_multi<false><<<n_planes, 256, 0, (cudaStream_t)stream>>>(static_cast<const VolDesc*>(desc_dev),
                                                                     reinterpret_cast<const int2*>(planes_dev),
                                                                     status_dev, cur_in_b & 1, flux_dev, csum_dev);
     note_launch();
@@ -353,18 +399,41 @@ constexpr long long STATIC_PLANES = 1 << 16;  // capacity of each half of the st
 // [0, STATIC_PLANES): per-plane flux sums; [STATIC_PLANES, 2*STATIC_PLANES): field sums.
 static __device__ __align__(256) double g_static_sums[2 * STATIC_PLANES];
 
-// Device address of g_static_sums per device, resolved once with that device current.
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+
+// The calling thread's current CUDA context (null if none yet or if the lookup fails).
+static CUcontext current_context() {
+    static CtxGetCurrentFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<CtxGetCurrentFn>(p);
+    });
+    CUcontext c = nullptr;
+    if (!fn || fn(&c) != CUDA_SUCCESS) return nullptr;
+    return c;
+}
+
+// Device address of g_static_sums on the current device, resolved with that device current the
+// first time and again whenever the device's context has changed (after a cudaDeviceReset the
+// module, and with it the array, is loaded anew).
 static double* static_sums_address() {
     constexpr int MAX_DEVICES = 64;
     static double* addr[MAX_DEVICES] = {nullptr};
+    static CUcontext ctx[MAX_DEVICES] = {nullptr};
     static std::mutex mu;
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return nullptr;
     std::lock_guard<std::mutex> lock(mu);
-    if (!addr[dev]) {
+    const CUcontext now = current_context();
+    if (!addr[dev] || !now || now != ctx[dev]) {
         void* p = nullptr;
         if (cudaGetSymbolAddress(&p, g_static_sums) != cudaSuccess) return nullptr;
         addr[dev] = static_cast<double*>(p);
+        ctx[dev] = current_context();
     }
     return addr[dev];
 }
@@ -382,14 +451,22 @@ extern "C" int tf_batch_converge_static(const void* desc_dev, const int32_t* pla
     // arena lengths the descriptor was built for (sum of nx-1, resp. nx, over the volumes)
     if (flux_len <= 0 || csum_len <= 0 || flux_len > STATIC_PLANES || csum_len > STATIC_PLANES)
         return TF_ERR_UNSUPPORTED;
+    // and they must be what tf_batch_describe actually built at desc_dev on this device: the
+    // offsets it wrote end within flux_len / csum_len, and n_vol does not exceed its volumes
+    DescExtent ext;
+    if (!find_extent(desc_dev, &ext) || ext.flux_end < 0 || n_vol > ext.n_vol || ext.flux_end > flux_len ||
+        ext.csum_end > csum_len)
+        return TF_ERR_ARG;
     double* sums = static_sums_address();
     if (!sums) return TF_ERR_CUDA;
     cudaStream_t st = (cudaStream_t)stream;
     // every sum the decision reads is written by the layer-sum launch of this same call, so
-    // nothing in the shared array has to start at zero
-    k_layer_sums_multi<<<n_planes, 256, 0, st>>>(static_cast<const VolDesc*>(desc_dev),
-                                                  reinterpret_cast<const int2*>(planes_dev), state.status,
-                                                  cur_in_b & 1, sums, sums + STATIC_PLANES);
+    // nothing in the shared array has to start at zero; the guarded kernel also skips plane items
+    // outside the descriptor's volumes and any index past the array
+    k_layer_sums_multi<true><<<n_planes, 256, 0, st>>>(static_cast<const VolDesc*>(desc_dev),
+                                                        reinterpret_cast<const int2*>(planes_dev), state.status,
+                                                        cur_in_b & 1, sums, sums + STATIC_PLANES, ext.n_vol,
+                                                        STATIC_PLANES, STATIC_PLANES);
     note_launch();
     if (cudaGetLastError() != cudaSuccess) return TF_ERR_CUDA;
     k_batch_check<<<n_vol, 32, 0, st>>>(static_cast<const VolDesc*>(desc_dev), n_vol, sums, state, conv_crit,

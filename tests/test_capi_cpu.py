@@ -82,6 +82,24 @@ def test_entry_points_reject_bad_arguments_without_launching(lib):
         _capi.check(_capi.TF_ERR_CUDA, "x")
 
 
+def test_static_scratch_entry_point_refuses_without_launching(lib):
+    """tf_batch_converge_static (the allocation-free convergence step) refuses missing state
+    pointers, arena lengths beyond its fixed array and a descriptor table that tf_batch_describe
+    never built, all before it launches anything."""
+    st = _capi.TfBatchState(*([16] * 9))
+    n0 = lib.tf_launch_count()
+    assert lib.tf_batch_converge_static(None, 16, 1, 1, 10, 10, st, 1e-2, 0, 0, None) == _capi.TF_ERR_ARG
+    assert lib.tf_batch_converge_static(16, None, 1, 1, 10, 10, st, 1e-2, 0, 0, None) == _capi.TF_ERR_ARG
+    assert lib.tf_batch_converge_static(16, 16, 0, 1, 10, 10, st, 1e-2, 0, 0, None) == _capi.TF_ERR_ARG
+    empty = _capi.TfBatchState(*([16] * 8 + [0]))
+    assert lib.tf_batch_converge_static(16, 16, 1, 1, 10, 10, empty, 1e-2, 0, 0, None) == _capi.TF_ERR_ARG
+    assert lib.tf_batch_converge_static(16, 16, 1, 1, 65537, 10, st, 1e-2, 0, 0, None) == _capi.TF_ERR_UNSUPPORTED
+    assert lib.tf_batch_converge_static(16, 16, 1, 1, 10, 65537, st, 1e-2, 0, 0, None) == _capi.TF_ERR_UNSUPPORTED
+    # a table address tf_batch_describe never filled (no device here either): refused
+    assert lib.tf_batch_converge_static(4096, 16, 1, 1, 10, 10, st, 1e-2, 0, 0, None) == _capi.TF_ERR_ARG
+    assert lib.tf_launch_count() == n0
+
+
 def test_anisotropic_divisors_match_reference_order():
     """LUT entries equal the reference's rolled sums on a volume exercising every pattern."""
     from oracle.sor import neighbour_counts
