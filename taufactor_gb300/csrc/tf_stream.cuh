@@ -23,6 +23,8 @@
 // x1 the margin planes are only read, never needed at a later time. Planes [x0, x1) are exact.
 #pragma once
 
+#include <mutex>
+
 #include "tf_common.cuh"
 #include "tf_internal.h"
 #include "tf_update.cuh"
@@ -346,6 +348,28 @@ inline int x_chunks_for(long long columns, int nx, int k, int slots) {
     return best;
 }
 
+// One-time set-up of a kernel on the current device: the dynamic shared-memory limit (an
+// attribute that applies to the device current when it is set) and the number of CTAs of the
+// kernel resident per SM. Kept per device and per kernel, guarded by a mutex; returns the
+// resident count, or 0 if the set-up failed (it is then tried again at the next call).
+template <auto KERN>
+static int prepare_kernel(int threads, int smem) {
+    constexpr int MAX_DEVICES = 64;
+    static std::mutex mu;
+    static int resident[MAX_DEVICES];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return 0;
+    std::lock_guard<std::mutex> lock(mu);
+    if (resident[dev] == 0) {
+        if (cudaFuncSetAttribute(KERN, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess) return 0;
+        int n = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, KERN, threads, smem) != cudaSuccess || n <= 0)
+            return 0;  // the kernel cannot run with this block on this device
+        resident[dev] = n;
+    }
+    return resident[dev];
+}
+
 template <int KIND, int TY, int TZ, int K, bool RHS>
 static int launch_stream(const tf_geom& gg, const tf_operator& op, const float* in, float* out, const uint8_t* code,
                          const float* rhs, int first_colour, int32_t* err, cudaStream_t st) {
@@ -357,17 +381,9 @@ static int launch_stream(const tf_geom& gg, const tf_operator& op, const float* 
     rc = encode_map_3d(&tmc, code, 1, gg.zhc, 2 * gg.yp, (long long)gg.batch * gg.nx, gg.zhc,
                        (long long)gg.zhc * 2 * gg.yp, S::WJC, 2 * S::ROWS);
     if (rc) return rc;
-    static bool attr_set = false;
-    static int resident = 1;  // CTAs of this kernel per SM
-    auto kern = k_stream<KIND, TY, TZ, K, RHS>;
-    if (!attr_set) {
-        if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, S::SMEM) != cudaSuccess)
-            return TF_ERR_CUDA;
-        int n = 0;
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, S::NT, S::SMEM) == cudaSuccess && n > 0)
-            resident = n;
-        attr_set = true;
-    }
+    constexpr auto kern = k_stream<KIND, TY, TZ, K, RHS>;
+    const int resident = prepare_kernel<kern>(S::NT, S::SMEM);  // CTAs of this kernel per SM
+    if (resident <= 0) return TF_ERR_CUDA;
     SweepArgs a = make_args(make_geo(gg), op, out, first_colour, K, err);
     a.rhs = rhs;
     const long long columns = (long long)((gg.nz + TZ - 1) / TZ) * ((gg.ny + TY - 1) / TY) * gg.batch;
