@@ -717,6 +717,9 @@ def run_profile(args):
     vols = batch_256(args.batch, args.side, SIGMA)
     cls = tg.PeriodicSolver if args.periodic else tg.Solver
     s = cls(vols, device="cuda")
+    if args.tile is not None:
+        from taufactor_gb300.autotune import apply
+        apply(s, args.tile, args.kmax)
     s._advance(8)
     torch.cuda.synchronize()
     s._advance(args.half_sweeps)
@@ -732,7 +735,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--tile", type=int, default=None, help="fixed tile shape instead of autotuning (0..2)")
+    ap.add_argument("--tile", type=int, default=None, help="fixed tile shape instead of autotuning (0..3)")
     ap.add_argument("--kmax", type=int, default=4, help="with --tile: half-sweeps per launch (1..4)")
     ap.add_argument("--profile", action="store_true", help="run the small profiler workload only")
     ap.add_argument("--batch", type=int, default=4, help="--profile: volumes")
