@@ -6,8 +6,8 @@ module level for plotting and surface metrics; none of them is used on the solve
 read-only source tree is left untouched.
 
 Only the golden-vector generator and the CPU oracle tests use this, and only where the source
-tree exists (``TAUFACTOR_REFERENCE`` or the default location below); it never runs on the GPU
-machine.
+tree exists: ``TAUFACTOR_REFERENCE`` names it, or else a directory ``reference`` beside the
+repository's own directory is used. It never runs on the GPU machine.
 """
 from __future__ import annotations
 
@@ -15,7 +15,9 @@ import os
 import sys
 import types
 
-DEFAULT_REFERENCE = "/root/reference"
+# a checkout of the reference beside this repository: <parent>/reference next to <parent>/<repo>
+DEFAULT_REFERENCE = os.path.join(os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))),
+                                 "reference")
 
 
 def reference_root() -> str | None:

@@ -30,14 +30,25 @@ def batch_256(n: int = 16, side: int = 256, sigma: float = 2.0, workers: int = 8
     return np.stack(vols)
 
 
-def uneven_volumes(n: int = 64, sides=(64, 96, 128, 192, 256), sigma: float = 2.0, workers: int = 8):
-    """n volumes with independently drawn sides (default_rng(2000)); volume i from default_rng(2001+i)."""
+def _uneven_draws(n: int, sides):
     rng = np.random.default_rng(2000)
     shapes = [tuple(int(s) for s in rng.choice(sides, 3)) for _ in range(n)]
     por = rng.uniform(0.35, 0.70, n)
+    return shapes, por
+
+
+def uneven_volumes(n: int = 64, sides=(64, 96, 128, 192, 256), sigma: float = 2.0, workers: int = 8):
+    """n volumes with independently drawn sides (default_rng(2000)); volume i from default_rng(2001+i)."""
+    shapes, por = _uneven_draws(n, sides)
     with cf.ThreadPoolExecutor(max_workers=workers) as ex:
         vols = list(ex.map(lambda i: blurred_noise(shapes[i], sigma, por[i], 2001 + i), range(n)))
     return vols
+
+
+def uneven_volume(i: int, n: int = 64, sides=(64, 96, 128, 192, 256), sigma: float = 2.0) -> np.ndarray:
+    """Volume i of ``uneven_volumes(n, sides, sigma)`` alone (same draws, same seed)."""
+    shapes, por = _uneven_draws(n, sides)
+    return blurred_noise(shapes[i], sigma, por[i], 2001 + i)
 
 
 def three_phase(side: int = 320, sigma: float = 3.0) -> np.ndarray:

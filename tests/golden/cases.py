@@ -195,3 +195,48 @@ IMPEDANCE_CASES = {
     "pimp_blob": (True, lambda: _imp_blob((16, 12, 10), 5), {}, {}, "electrode.py:369-402"),
     "pimp_odd": (True, lambda: _imp_blob((14, 9, 11), 6, inert=0.2), {}, {}, "electrode.py:369-402"),
 }
+
+
+# Full-size cases of the benchmark configurations, solved by the reference itself on the host
+# (``make_golden.py fullsize``; minutes each). name -> (kind, input builder, constructor kwargs,
+# solve kwargs, what it is). Only scalars and the [Nx-1] layer flux are stored; the GPU tests
+# regenerate the volumes from their seeds.
+def c2_volume0():
+    from taufactor_gb300.synthetic import batch_256
+
+    return batch_256(n=1, workers=1)[0]
+
+
+def c3_volume15():
+    from taufactor_gb300.synthetic import uneven_volume
+
+    return uneven_volume(15)  # 256 x 256 x 192, the largest PeriodicSolver volume of the batch
+
+
+def c4_crop128():
+    from taufactor_gb300.synthetic import three_phase
+
+    return three_phase(320)[:128, :128, :128]
+
+
+def blur64():
+    from taufactor_gb300.synthetic import blurred_noise
+
+    return blurred_noise((64, 64, 64), 2.0, 0.5, 77)
+
+
+FULLSIZE_CASES = {
+    "c2_v0_cc2": ("binary", c2_volume0, {}, {"conv_crit": 1e-2}, "16 x 256^3 workload, volume 0"),
+    "c2_v0_cc4": ("binary", c2_volume0, {}, {"conv_crit": 1e-4}, "16 x 256^3 workload, volume 0"),
+    "c3_v15_periodic": ("periodic", c3_volume15, {}, {"conv_crit": 1e-4}, "uneven batch, volume 15"),
+    "c4_crop128": ("multiphase", c4_crop128, {"diffusivities": {0: 0.0, 1: 1.0, 2: 0.1}},
+                   {"conv_crit": 1e-4}, "three-label 320^3 volume, first 128^3"),
+}
+
+# The reference's precision argument (taufactor.py:24, :33): float64 sweeps.
+# name -> (kind, input builder, solve kwargs)
+DOUBLE_CASES = {
+    "f64_bernoulli100": ("binary", bernoulli_100, {"conv_crit": 2e-2}),
+    "f64_blur64": ("binary", blur64, {"conv_crit": 1e-4}),
+    "f64_blur64_periodic": ("periodic", blur64, {"conv_crit": 1e-4}),
+}
