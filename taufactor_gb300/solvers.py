@@ -68,13 +68,23 @@ class SORSolver:
     #: set to a list to record (start event, end event, half-sweeps) around every tf_advance call
     event_log = None
 
+    #: hooks of the reference's SORSolver (taufactor.py:70-103) whose arithmetic this package runs
+    #: in its own CUDA kernels; a subclass overriding one would be ignored there, so it is refused
+    DEVICE_HOOKS = ("return_mask", "init_field", "init_conductive_neighbours", "init_reactive_neighbours",
+                    "apply_boundary_conditions", "sum_weighted_neighbours", "vertical_flux")
+
     def __init__(self, img: np.ndarray, omega: float | None = None, precision=None, device="cuda"):
+        self._refuse_overridden_hooks()
         self.cpu_img = self._expand_to_4d(img)
         self.batch_size, self.Nx, self.Ny, self.Nz = self.cpu_img.shape
+        # taufactor.py:33: the dtype of the sweeps. Here the sweeps are float32 either way; with
+        # torch.float64 every solve ends with a float64 defect correction (refine) and the
+        # metrics and `field` are those of the float64 solution.
+        if precision not in (None, torch.float32, torch.float64):
+            raise ValueError("precision must be None, torch.float32 or torch.float64 "
+                             f"(got {precision!r})")
+        self.precision = torch.float64 if precision == torch.float64 else torch.float32
         self.device = self._init_device(device)
-        if precision not in (None, torch.float32):
-            raise ValueError("taufactor_gb300 sweeps in float32; precision must be None or torch.float32")
-        self.precision = torch.float32
         if omega is None:
             omega = 2 - math.pi / (1.5 * self.Nx)  # taufactor.py:36-37
         self.omega = omega
@@ -94,6 +104,18 @@ class SORSolver:
         self.tau_x = None
         self.D_eff = None
         self.walltime = 0.0
+
+    @classmethod
+    def _refuse_overridden_hooks(cls):
+        own = __name__.split(".")[0]
+        for name in cls.DEVICE_HOOKS:
+            fn = getattr(cls, name, None)
+            if fn is not None and not (getattr(fn, "__module__", None) or "").startswith(own):
+                raise NotImplementedError(
+                    f"{cls.__name__}.{name} overrides a hook of the reference's SORSolver; taufactor_gb300 "
+                    "computes the operator in its own CUDA kernels and cannot call it. Express the operator "
+                    "through MultiPhaseSolver (per-label diffusivities), AnisotropicSolver or KappaSolver "
+                    "(per-voxel conductivity), or use the reference package for custom hooks.")
 
     # ------------------------------------------------------------------ hooks
     def _device_labels(self):
@@ -308,13 +330,63 @@ class SORSolver:
 
     @property
     def field(self) -> torch.Tensor:
-        """The concentration field in the reference's padded layout [B,Nx+2,Ny+2,Nz+2] (a copy)."""
+        """The concentration field in the reference's padded layout [B,Nx+2,Ny+2,Nz+2] (a copy).
+
+        float32; with precision=torch.float64 and a float64 solution present (after refine), the
+        float64 field with the same ghost planes."""
         out = torch.empty((self.batch_size, self.Nx + 2, self.Ny + 2, self.Nz + 2), dtype=torch.float32,
                           device=self.device)
         with torch.cuda.device(self.device):
             check(self._lib.tf_unpack(C.byref(self._geom), C.byref(self._op), _ptr(self._cur), _ptr(out),
                                       self._stream()), "tf_unpack")
+            if self.precision != torch.float64 or self._field64 is None:
+                return out
+            nat = torch.empty((self.batch_size, self.Nx, self.Ny, self.Nz), dtype=torch.float64, device=self.device)
+            check(self._lib.tf_split_to_natural_f64(C.byref(self._geom), _ptr(self._field64), _ptr(nat),
+                                                    self._stream()), "tf_split_to_natural_f64")
+            out = out.double()
+            out[:, 1:-1, 1:-1, 1:-1] = nat
+            if self._periodic:  # ghost copies as the reference's apply_boundary_conditions (:501-505)
+                out[:, :, 0, :] = out[:, :, -2, :]
+                out[:, :, -1, :] = out[:, :, 1, :]
+                out[:, :, :, 0] = out[:, :, :, -2]
+                out[:, :, :, -1] = out[:, :, :, 1]
         return out
+
+    # ------------------------------------------------------------------ operator tensors
+    # The reference keeps its operator as tensors (taufactor.py:43-67): the divisor `factor`
+    # [B,Nx,Ny,Nz] (inf where a voxel is frozen), the over-relaxation chequerboards `cb` and,
+    # for the multiphase solvers, the face diffusivities D_x, D_y, D_z. The kernels here never
+    # form them; they are built on first access, on the device, with the reference's formulas.
+    @property
+    def cb(self):
+        """[omega * cb, omega * (1 - cb)] with cb = 1 where (x + y + z) is even (taufactor.py:218-225)."""
+        cached = getattr(self, "_cb_tensors", None)
+        if cached is None:
+            dev = self.device
+            par = (torch.arange(self.Nx, device=dev)[:, None, None] + torch.arange(self.Ny, device=dev)[None, :, None]
+                   + torch.arange(self.Nz, device=dev)[None, None, :]) % 2
+            w = torch.tensor(self.omega, dtype=torch.float64, device=dev)
+            zero = torch.zeros((), dtype=torch.float64, device=dev)
+            cached = [torch.where(par == 0, w, zero).to(self.precision), torch.where(par == 1, w, zero).to(self.precision)]
+            self._cb_tensors = cached
+        return cached
+
+    @property
+    def factor(self) -> torch.Tensor:
+        """The divisor of the update per voxel, [B,Nx,Ny,Nz] (inf = frozen), as the reference's
+        init_conductive_neighbours returns it for this solver class."""
+        cached = getattr(self, "_factor_tensor", None)
+        if cached is None:
+            cached = self._build_factor()
+            self._factor_tensor = cached
+        return cached
+
+    def _labels_tensor(self) -> torch.Tensor:
+        return torch.from_numpy(np.ascontiguousarray(self.cpu_img)).to(self.device).to(self.precision)
+
+    def _build_factor(self) -> torch.Tensor:
+        raise NotImplementedError(f"{type(self).__name__} has no divisor tensor")
 
     @field.setter
     def field(self, value: torch.Tensor):
@@ -371,6 +443,13 @@ class SORSolver:
             torch.cuda.reset_peak_memory_stats(device=self.device)
         if verbose == "debug":
             self.tau_t = []
+        double = self.precision == torch.float64
+        if double:
+            # float32 sweeps to the reference's rule (flux spreads below ~1e-5 are beyond a
+            # float32 field), then the float64 correction
+            conv_crit = max(conv_crit, 1e-5)
+            if not refine:
+                refine = True
         start = timer()
         while not self.converged and self.iter < iter_limit:
             n = min(100 - self.iter % 100, iter_limit - self.iter)
@@ -378,7 +457,10 @@ class SORSolver:
             if self.iter % 100 == 0:
                 self.converged = self.check_convergence(verbose, conv_crit, plot_interval)
         if refine:
-            self.refine(**(refine if isinstance(refine, dict) else {}))
+            hist = self.refine(**(refine if isinstance(refine, dict) else {}))
+            if double:
+                self.converged = bool(self.converged and hist[-1] < (refine.get("tol", 1e-10)
+                                                                      if isinstance(refine, dict) else 1e-10))
         torch.cuda.synchronize(self.device)
         self.walltime = timer() - start
         self._end_simulation(self.iter, verbose)
@@ -528,6 +610,10 @@ def layer_metrics(s, flux_1d: np.ndarray, c_x_raw: np.ndarray):
 class Solver(ThroughTransportSolver):
     """Two-phase solver: 1 = conductive, 0 = not (taufactor.py:355-419)."""
 
+    # a subclass that builds itself through ThroughTransportSolver.__init__ (as the reference's
+    # float64 pattern does) has run the reference's host label check itself
+    _labels_checked = True
+
     def __init__(self, img, omega=None, D_0=1, device="cuda"):
         self._labels_checked = not self._labels_go_to_device(img, device)
         if self._labels_checked:
@@ -606,6 +692,27 @@ class Solver(ThroughTransportSolver):
         for n in range(1, 9):
             op.divisor[n] = float(n)
         return op
+
+    def _build_factor(self):
+        """Conductive face neighbours, the Dirichlet x-faces counted 2, weighted by (1, Ky, Kz)
+        for AnisotropicSolver; y/z wrap for the periodic class (taufactor.py:402-410, :459-471,
+        :493-499)."""
+        img = self._labels_tensor()
+        w = (1.0, getattr(self, "Ky", 1.0), getattr(self, "Kz", 1.0))
+        p = torch.nn.functional.pad(img, (1, 1, 1, 1, 1, 1))
+        p[:, 0], p[:, -1] = 2, 2
+        p[:, :, 0], p[:, :, -1] = 0, 0
+        p[:, :, :, 0], p[:, :, :, -1] = 0, 0
+        if self._periodic:
+            p = p[:, :, 1:-1, 1:-1]
+        nn = torch.zeros_like(p)
+        for dim in range(1, 4):
+            for dr in (1, -1):
+                nn += torch.roll(p, dr, dim) * w[dim - 1] if dim > 1 and w[dim - 1] != 1.0 else torch.roll(p, dr, dim)
+        nn = nn[:, 1:-1] if self._periodic else nn[:, 1:-1, 1:-1, 1:-1]
+        nn[img == 0] = torch.inf
+        nn[nn == 0] = torch.inf
+        return nn
 
 
 class PeriodicSolver(Solver):
@@ -728,6 +835,58 @@ class MultiPhaseSolver(ThroughTransportSolver):
                 op.face[a * 32 + b] = float(harmonic_face(d[a], d[b]))
         return op
 
+
+    def _face_tensors(self):
+        """(D_x, D_y, D_z): harmonic-mean face diffusivities as the reference builds them
+        (taufactor.py:577-596; periodic wrap :626-650), [B,Nx+1,Ny,Nz], [B,Nx,Ny+1,Nz], [B,Nx,Ny,Nz+1]."""
+        cached = getattr(self, "_faces_cache", None)
+        if cached is not None:
+            return cached
+        img = self._labels_tensor()
+        dmap = torch.zeros_like(img)
+        for phase, D_p in self.Ds.items():
+            dmap[img == phase] = D_p
+        d = torch.nn.functional.pad(dmap, (1, 1, 1, 1, 1, 1))
+        d[:, 0] = d[:, 1]
+        d[:, -1] = d[:, -2]
+        if self._periodic:
+            d[:, :, 0, :] = d[:, :, -2, :]
+            d[:, :, -1, :] = d[:, :, 1, :]
+            d[:, :, :, 0] = d[:, :, :, -2]
+            d[:, :, :, -1] = d[:, :, :, 1]
+
+        def hm(a, b):
+            den = a + b
+            out = torch.zeros_like(den)
+            ok = den > 0
+            out[ok] = 2 * a[ok] * b[ok] / den[ok]
+            return out
+
+        cached = (hm(d[:, :-1, 1:-1, 1:-1], d[:, 1:, 1:-1, 1:-1]), hm(d[:, 1:-1, :-1, 1:-1], d[:, 1:-1, 1:, 1:-1]),
+                  hm(d[:, 1:-1, 1:-1, :-1], d[:, 1:-1, 1:-1, 1:]))
+        self._faces_cache = cached
+        return cached
+
+    @property
+    def D_x(self) -> torch.Tensor:
+        return self._face_tensors()[0]
+
+    @property
+    def D_y(self) -> torch.Tensor:
+        return self._face_tensors()[1]
+
+    @property
+    def D_z(self) -> torch.Tensor:
+        return self._face_tensors()[2]
+
+    def _build_factor(self):
+        """Sum of the six faces plus the extra Dirichlet x-face, 0 -> inf (taufactor.py:598-604)."""
+        D_x, D_y, D_z = self._face_tensors()
+        factor = D_x[:, :-1] + D_x[:, 1:] + D_y[:, :, :-1] + D_y[:, :, 1:] + D_z[:, :, :, :-1] + D_z[:, :, :, 1:]
+        factor[:, 0] += D_x[:, 0]
+        factor[:, -1] += D_x[:, -1]
+        factor[factor == 0] = torch.inf
+        return factor
 
     def phase_gradients(self, conv_crit: float = 1e-3, tol: float = 1e-11) -> dict:
         """dD_eff/dD_p for every label p (numpy [B] per label), by the adjoint method.
