@@ -8,7 +8,7 @@ constructor and ``solve()`` surface. The sweeps run as hand-written CUDA kernels
 its C ABI (``include/taufactor_gb300.h``). ``read_tiff`` loads the multi-page TIFF volumes the
 reference's examples read with ``tifffile.imread`` (README.md:51-55).
 """
-from .batch import BatchSolve
+from .batch import BatchSolve, MultiDeviceBatchSolve, split_volumes
 from .kappa import DeffFunction, KappaSolver, d_eff
 from .solvers import (AnisotropicSolver, ElectrodeSolver, MultiPhaseSolver, PeriodicElectrodeSolver,
                       PeriodicMultiPhaseSolver, PeriodicSolver, SORSolver, Solver, ThroughTransportSolver)
@@ -17,6 +17,6 @@ from .tiff import read_tiff, write_tiff
 
 __all__ = ["Solver", "PeriodicSolver", "AnisotropicSolver", "MultiPhaseSolver", "PeriodicMultiPhaseSolver",
            "ElectrodeSolver", "PeriodicElectrodeSolver", "ImpedanceSolver", "PeriodicImpedanceSolver",
-           "SORSolver", "ThroughTransportSolver", "BatchSolve", "KappaSolver", "DeffFunction", "d_eff",
+           "SORSolver", "ThroughTransportSolver", "BatchSolve", "MultiDeviceBatchSolve", "split_volumes", "KappaSolver", "DeffFunction", "d_eff",
            "read_tiff", "write_tiff"]
 __version__ = "0.1.0"

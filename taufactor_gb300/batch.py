@@ -471,3 +471,69 @@ class BatchSolve:
                 res.residual_history = hist[v]
             self.c64 = c64
         return self.results
+
+
+def split_volumes(sizes, n_parts: int):
+    """Whole volumes to `n_parts` devices, balanced by voxel count: largest first, each to the
+    part with the fewest voxels so far (ties to the lower part). Returns one sorted index list
+    per part; every index appears exactly once. The volumes are independent, so no part ever
+    waits for another (the natural shard of a batch of volumes)."""
+    if n_parts < 1:
+        raise ValueError("n_parts must be >= 1")
+    load = [0] * n_parts
+    parts = [[] for _ in range(n_parts)]
+    for i in sorted(range(len(sizes)), key=lambda i: (-int(sizes[i]), i)):
+        p = min(range(n_parts), key=lambda j: (load[j], j))
+        parts[p].append(i)
+        load[p] += int(sizes[i])
+    return [sorted(p) for p in parts]
+
+
+class MultiDeviceBatchSolve:
+    """BatchSolve over several GPUs of one process: whole volumes per device (split_volumes),
+    one BatchSolve per device, driven from one host thread each; results come back in the
+    caller's order. No data crosses devices (each volume lives on one GPU)."""
+
+    def __init__(self, volumes, devices, periodic=False, omega=None):
+        vols = [np.asarray(v) for v in volumes]
+        n = len(vols)
+        per = list(periodic) if isinstance(periodic, (list, tuple, np.ndarray)) else [bool(periodic)] * n
+        om = list(omega) if isinstance(omega, (list, tuple, np.ndarray)) else [omega] * n
+        if len(per) != n or len(om) != n:
+            raise ValueError("periodic / omega must give one entry per volume")
+        self.devices = [torch.device(d) for d in devices]
+        self.parts = [p for p in split_volumes([v.size for v in vols], len(self.devices))]
+        self.batches = [BatchSolve([vols[i] for i in p], periodic=[per[i] for i in p], omega=[om[i] for i in p],
+                                   device=d) if p else None for p, d in zip(self.parts, self.devices)]
+        self.n = n
+
+    def solve(self, **kwargs):
+        import threading
+
+        errors = []
+
+        def run(b):
+            try:
+                b.solve(**kwargs)
+            except BaseException as e:  # re-raised on the calling thread
+                errors.append(e)
+
+        threads = [threading.Thread(target=run, args=(b,)) for b in self.batches if b is not None]
+        start = timer()
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        self.walltime = timer() - start
+        if errors:
+            raise errors[0]
+        return self.results
+
+    @property
+    def results(self):
+        out = [None] * self.n
+        for p, b in zip(self.parts, self.batches):
+            if b is not None:
+                for j, i in enumerate(p):
+                    out[i] = b.results[j]
+        return out
