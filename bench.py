@@ -77,6 +77,69 @@ def cpu_baseline(pool, workers):
                              "cores": workers}
 
 
+# ----------------------------------------------------------------------------- the reference itself
+REF_HALF_SWEEPS = 100  # one sample: 100 half-sweeps, i.e. one convergence check of the reference
+
+
+def reference_module():
+    """The reference package installed under baseline/_ref (its plotting imports stubbed), or None."""
+    from oracle.ref_shim import import_reference
+
+    return import_reference(os.path.join(ROOT, "baseline", "_ref"))
+
+
+def workload_volume(i: int) -> np.ndarray:
+    """Volume i of the 16 x 256^3 workload, alone (the same draws as synthetic.batch_256)."""
+    from taufactor_gb300.synthetic import blurred_noise
+
+    por = np.random.default_rng(999).uniform(0.35, 0.70, i + 1)[i]
+    return blurred_noise((SIDE,) * 3, SIGMA, por, 1000 + i)
+
+
+def reference_cpu_sample(tau, i: int, half_sweeps: int = REF_HALF_SWEEPS):
+    """The reference's own Solver(device='cpu') on volume i (taufactor.py:380-385, :156-191):
+    set-up, then solve(iter_limit=half_sweeps). Returns (solve s, set-up s, half-sweeps done)."""
+    import contextlib
+    import io
+
+    vol = workload_volume(i)
+    with contextlib.redirect_stdout(io.StringIO()):  # its "not converged" notice
+        t0 = time.perf_counter()
+        s = tau.Solver(vol, device="cpu")
+        t1 = time.perf_counter()
+        s.solve(iter_limit=half_sweeps, verbose=False, conv_crit=CONV_CRIT)
+        t2 = time.perf_counter()
+    return t2 - t1, t1 - t0, int(s.iter)
+
+
+def reference_cuda_rate(tau, half_sweeps: int = 200):
+    """The reference's own torch-eager GPU path (device='cuda') on the whole 16 x 256^3 batch:
+    voxel-updates/s of solve(iter_limit=half_sweeps) after a 100-half-sweep warm-up solve."""
+    import contextlib
+    import io
+
+    import torch
+
+    from taufactor_gb300.synthetic import batch_256
+
+    vols = batch_256(N_VOL, SIDE, SIGMA)
+    with contextlib.redirect_stdout(io.StringIO()):
+        s = tau.Solver(vols, device="cuda")
+        s.solve(iter_limit=100, verbose=False, conv_crit=CONV_CRIT)
+        s = tau.Solver(vols, device="cuda")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.solve(iter_limit=half_sweeps, verbose=False, conv_crit=CONV_CRIT)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+    rate = s.iter * vols.size / 2 / dt
+    del s
+    torch.cuda.empty_cache()
+    return {"value": rate, "unit": UNIT, "half_sweeps": half_sweeps,
+            "what": "the reference's Solver(device='cuda') (torch eager) on the same 16 x 256^3 batch, "
+                    "solve(iter_limit=200) after a warm-up solve; informational"}
+
+
 # ----------------------------------------------------------------------------- clocks
 class ClockSampler:
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -142,9 +205,48 @@ def measured_peak_hbm():
 
 # ----------------------------------------------------------------------------- arms
 def run_reference(args):
+    """The reference arm: the reference's own CPU Solver on the host cores (baseline/_ref), each
+    step one bounded sample of the workload (volume step % 16, set-up excluded, 100 half-sweeps
+    with the reference's convergence check); without an installed reference, the oracle's numpy
+    restatement of its op sequence (kind "port"). Rank 0 only."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
+    tau = reference_module()
+    if tau is None:
+        return run_reference_port(args)
+    import torch
+
+    cores = os.cpu_count() or 1
+    torch.set_num_threads(cores)
+    V = SIDE ** 3
+    for w in range(args.warmup):
+        reference_cpu_sample(tau, w % N_VOL, 10)
+    rates, setups = [], []
+    for j in range(args.steps):
+        dt, ts, n = reference_cpu_sample(tau, j % N_VOL)
+        rates.append(n * V / 2 / dt)
+        setups.append(ts)
+    v = float(np.median(rates))
+    sample = (f"taufactor {getattr(tau, '__version__', '1.2.1')} Solver(device='cpu'), torch {torch.__version__} "
+              f"with {cores} threads: per step one 256^3 volume of the workload (volume step % {N_VOL}), "
+              f"solve(iter_limit={REF_HALF_SWEEPS}) timed after set-up (set-up median "
+              f"{float(np.median(setups)):.2f} s)")
+    out = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": workload_config(),
+           "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "reference", "sample": sample},
+           "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    if torch.cuda.is_available() and not getattr(args, "no_reference_cuda", False):
+        try:
+            out["reference_torch_cuda"] = reference_cuda_rate(tau)
+        except Exception as e:  # informational only
+            out["reference_torch_cuda"] = {"unavailable": f"{type(e).__name__}: {e}"}
+    print(json.dumps(out), flush=True)
+
+
+def run_reference_port(args):
+    """Reference arm without an installed reference: the oracle's float32 restatement."""
     workers = min(N_VOL, os.cpu_count() or 1)
     ctx = mp.get_context("spawn")
     with ctx.Pool(workers) as pool:
@@ -164,6 +266,42 @@ def run_reference(args):
            "cpu_baseline": {"value": v, "unit": UNIT, "cores": workers, "kind": "port", "sample": sample},
            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out), flush=True)
+
+
+def rank_volumes(rank: int, n: int = N_VOL) -> range:
+    """Indices in the seeded volume sequence that rank `rank` solves: its own n consecutive
+    volumes, so rank 0's batch is the single-GPU workload and no two ranks share a volume."""
+    return range(rank * n, rank * n + n)
+
+
+def _rank_entry(local: int, world: int, port: int, target, targs):
+    """One process of a self-launched multi-GPU run: the environment torchrun would give it."""
+    os.environ.update(RANK=str(local), LOCAL_RANK=str(local), WORLD_SIZE=str(world), MASTER_ADDR="127.0.0.1",
+                      MASTER_PORT=str(port))
+    target(*targs)
+
+
+def spawn_ranks(world: int, target, *targs):
+    """Run target(*targs) in `world` processes with RANK / LOCAL_RANK / WORLD_SIZE / MASTER_*
+    set as torchrun sets them (rendezvous on 127.0.0.1, a free port)."""
+    import socket
+
+    import torch.multiprocessing as tmp
+
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    tmp.spawn(_rank_entry, args=(world, port, target, targs), nprocs=world, join=True)
+
+
+def check_world(gpus: int, env=None) -> bool:
+    """True when this process must launch the ranks itself (--gpus N > 1 without torchrun);
+    a WORLD_SIZE that disagrees with --gpus is an error."""
+    env = os.environ if env is None else env
+    ws = env.get("WORLD_SIZE")
+    if ws is not None and int(ws) != gpus:
+        raise SystemExit(f"bench.py: WORLD_SIZE={ws} but --gpus {gpus}; launch exactly one rank per GPU")
+    return ws is None and gpus > 1
 
 
 def combine_ranks(ms: float, units: float, world: int, device=None):
@@ -187,8 +325,9 @@ def run_ours(args):
     local = int(os.environ.get("LOCAL_RANK", "0"))
     pool = None
     workers = min(N_VOL, os.cpu_count() or 1)
-    if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        # started before any CUDA call (spawned workers never touch the GPU)
+    ref_tau = reference_module() if (rank == 0 and world == 1 and not args.no_cpu_baseline) else None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline and ref_tau is None:
+        # the oracle port instead; started before any CUDA call (spawned workers never touch the GPU)
         pool = mp.get_context("spawn").Pool(workers)
     import torch
 
@@ -202,7 +341,7 @@ def run_ours(args):
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=dev)
-    vols = batch_256(N_VOL, SIDE, SIGMA, first=rank * N_VOL)  # each rank its own volumes
+    vols = batch_256(N_VOL, SIDE, SIGMA, first=rank_volumes(rank).start)  # each rank its own volumes
     V = vols.size  # voxels in this rank's batch
 
     def barrier():
@@ -276,11 +415,23 @@ def run_ours(args):
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     e2e_value = e2e_steps * e2e_iters * V / 2 / e2e_s
+    secondary = None
+    if rank == 0 and world == 1 and not args.no_secondary:
+        secondary = secondary_metrics(dev)
     cpu = None
     if pool is not None:
         rate, info = cpu_baseline(pool, workers)
         pool.close()
         cpu = {"value": rate, "unit": UNIT, "cores": info["cores"], "kind": "port", "sample": info["sample"]}
+    elif ref_tau is not None:
+        cores = os.cpu_count() or 1
+        torch.set_num_threads(cores)
+        reference_cpu_sample(ref_tau, 0, 10)  # warm-up
+        samples = [reference_cpu_sample(ref_tau, i) for i in range(2)]
+        rate = float(np.median([n * SIDE ** 3 / 2 / dt for dt, _, n in samples]))
+        cpu = {"value": rate, "unit": UNIT, "cores": cores, "kind": "reference",
+               "sample": f"the reference's Solver(device='cpu') on volumes 0 and 1 of the workload, "
+                         f"solve(iter_limit={REF_HALF_SWEEPS}) after set-up, torch with {cores} threads"}
     if rank != 0:
         if world > 1:
             torch.distributed.destroy_process_group()
@@ -308,9 +459,34 @@ def run_ours(args):
     }
     if cpu:
         out["cpu_baseline"] = cpu
+    if secondary:
+        out.update(secondary)
     print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def secondary_metrics(dev):
+    """The metric's other parts, on the same GPU after the main measurement: converged solves/s of
+    the 64-volume uneven batch against the per-volume loop (FP32, and FP32 + FP64 correction to a
+    relative residual of 1e-4), and the adjoint/forward time with a central-difference check of
+    the gradient on 8 voxels of the 320^3 per-voxel conductivity field."""
+    u = uneven_batch(dev, repeat=1, refine_tols=(1e-4,), reference_tol=1e-10)
+    r4 = u["refined"]["0.0001"]
+    a = adjoint_cost(dev, side=320, fd_voxels=8, phases=False)
+    return {
+        "uneven_batch": {"workload": u["workload"], "batched_solves_per_s": u["batched_solves_per_s"],
+                         "per_volume_loop_solves_per_s": u["per_volume_loop_solves_per_s"],
+                         "speedup_vs_loop": u["speedup"], "refined_1e-4_solves_per_s": r4["solves_per_s"],
+                         "refined_1e-4_speedup_vs_loop": r4["speedup_vs_loop"],
+                         "max_rel_D_eff_vs_fp64": u["max_rel_D_eff_loop_vs_fp64"],
+                         "refined_1e-4_max_rel_D_eff_vs_fp64": r4["max_rel_D_eff_vs_fp64"],
+                         "max_rel_D_eff_batched_vs_loop": u["max_rel_D_eff_batched_vs_loop"]},
+        "adjoint": {"workload": a["workload"], "forward_s": a["forward_s"], "adjoint_s": a["adjoint_s"],
+                    "adjoint_over_forward": a["adjoint_over_forward"], "fd_voxels": a["fd_voxels"],
+                    "fd_h": a["fd_h"], "fd_max_rel_err": a["fd_max_rel_err"],
+                    "fd_direction_rel_err": a["fd_direction_rel_err"], "euler_rel_err": a["euler_rel_err"]},
+    }
 
 
 def uneven_batch(dev, conv_crit=CONV_CRIT, repeat=2, refine_tols=(1e-4, 1e-6, 1e-8), reference_tol=1e-10):
@@ -586,7 +762,7 @@ def impedance_throughput(dev, side=256, nyq_side=64, cpu_half_sweeps=4):
                         "max_rel_diff_converged": float(max(agree)) if agree else None}}
 
 
-def adjoint_cost(dev, side=320, fd_voxels=0, tol=1e-12, fd_tol=1e-14):
+def adjoint_cost(dev, side=320, fd_voxels=0, tol=1e-12, fd_tol=1e-14, phases=True):
     """Per-voxel conductivity kappa = sigmoid(blur_2(2 N(0,1))) on side^3 (default_rng(3003)):
     forward solve + FP64 refinement, then the adjoint gradient; times and, with fd_voxels > 0,
     central finite differences (h = 1e-3) on random voxels (default_rng(3004))."""
@@ -622,6 +798,8 @@ def adjoint_cost(dev, side=320, fd_voxels=0, tol=1e-12, fd_tol=1e-14):
     # faces (the float32 faces of MultiPhaseSolver's own refined D_eff move in rounding steps that
     # dominate a difference of step 1e-3). D_0 = 0 is a one-sided point: a phase of zero
     # conductivity is not part of the system, so no central difference exists there.
+    if not phases:
+        return _adjoint_fd(out, s, g, kap, side, fd_voxels, fd_tol, dev) if fd_voxels else out
     from taufactor_gb300.synthetic import three_phase
 
     lab = three_phase(side)
@@ -653,6 +831,14 @@ def adjoint_cost(dev, side=320, fd_voxels=0, tol=1e-12, fd_tol=1e-14):
         fd = (dd[0] - dd[1]) / hp
         phase[f"fd_rel_err_phase{p}"] = abs(fd - float(pg[p][0])) / abs(fd)
     out["multiphase_320"] = phase
+    return _adjoint_fd(out, s, g, kap, side, fd_voxels, fd_tol, dev) if fd_voxels else out
+
+
+def _adjoint_fd(out, s, g, kap, side, fd_voxels, fd_tol, dev):
+    """Central differences (h = 1e-3) of D_eff on random voxels and along a random direction,
+    against the adjoint gradient g of solver s."""
+    import taufactor_gb300 as tg
+
     if fd_voxels:
         def deff(kk):
             t = tg.KappaSolver(kk, device=dev)
@@ -735,6 +921,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true", help="skip the uneven-batch and adjoint measurements")
+    ap.add_argument("--no-reference-cuda", action="store_true",
+                    help="--impl reference: skip the reference's own GPU path")
     ap.add_argument("--tile", type=int, default=None, help="fixed tile shape instead of autotuning (0..3)")
     ap.add_argument("--kmax", type=int, default=4, help="with --tile: half-sweeps per launch (1..4)")
     ap.add_argument("--profile", action="store_true", help="run the small profiler workload only")
@@ -767,6 +956,8 @@ def main():
             print(json.dumps(adjoint_cost(dev, args.adj_side, args.fd_voxels)), flush=True)
     elif args.profile:
         run_profile(args)
+    elif check_world(args.gpus):
+        spawn_ranks(args.gpus, run_reference if args.impl == "reference" else run_ours, args)
     elif args.impl == "reference":
         run_reference(args)
     else:
