@@ -1,7 +1,8 @@
 """Autotuner for the fused sweep kernel: tile shape and half-sweeps per launch.
 
-The fused kernel has three tile shapes (16x64, 16x128, 32x64 rows x z-cells) and fuses 1..4
-half-sweeps per launch; which pair is fastest depends on the volume's shape and the GPU. The
+The fused kernel has four tile shapes (16x64, 16x128, 32x64 rows x z-cells, and 16x128 row
+pairs for even fused depths) and fuses 1..4 half-sweeps per launch; which pair is fastest
+depends on the volume's shape and the GPU. The
 tuner times every candidate on the solver's own volumes with CUDA events (a few launches
 each), restores the field afterwards and keeps the fastest. Results are cached per
 (operator, shape, batch, device) in memory and, if ``TAUFACTOR_GB300_CACHE`` names a file, on
@@ -15,7 +16,7 @@ import os
 
 import torch
 
-CANDIDATES = [(tile, k) for k in (4, 3, 2) for tile in (0, 1, 2)]
+CANDIDATES = [(tile, k) for k in (4, 3, 2) for tile in (0, 1, 2)] + [(3, 4), (3, 2)]
 _MEMO: dict = {}
 
 

@@ -24,6 +24,8 @@
 // (taufactor.py:95-103, :174-182).
 #pragma once
 
+#include <type_traits>
+
 #include "tf_stream.cuh"
 
 namespace tf {
@@ -41,24 +43,26 @@ struct RowPairShape {
     static constexpr int NHALO = 2 * HG * NP;          // halo threads
     static constexpr int NW = NP * WM + (NHALO + 31) / 32;
     static constexpr int NT = 32 * NW;
-    static constexpr int R = K + 2;                    // planes held in registers
-    static constexpr int D = 3;                        // planes loaded ahead
-    static constexpr int NS = K + 1 + D;               // shared-memory slots
-    static constexpr int FBYTES = 2 * ROWS * WJ * 4;
+    static constexpr int R = K + 2;                    // planes held in registers = ring slots in shared memory
+    static constexpr int D = R / 2;                    // TMA staging buffers (D - 1 planes in flight ahead)
+    static constexpr int FBYTES = 2 * ROWS * WJ * 4;   // one staged plane of the field
+    static constexpr int CBYTES = 2 * ROWS * WJC;      // one staged plane of the codes
     static constexpr int GUARD = (2 * WJ * 4 + 127) / 128 * 128;  // one zero row (both half-rows)
-    static constexpr int FSTRIDE = (FBYTES + 127) / 128 * 128 + GUARD;
-    static constexpr int CBYTES = 2 * ROWS * WJC;
-    static constexpr int CSTRIDE = (CBYTES + 127) / 128 * 128;
-    static constexpr int LUT_BYTES = (DIV_TABLE_BYTES + 127) / 128 * 128;
-    static constexpr int HEAD = 128 + LUT_BYTES;       // mbarriers + failure flag, division table
-    static constexpr int FIELD0 = HEAD + GUARD;        // slot s: FIELD0 + s * FSTRIDE, a guard on each side
-    static constexpr int CODE0 = FIELD0 + NS * FSTRIDE;
-    static constexpr int SMEM = CODE0 + NS * CSTRIDE;
+    static constexpr int RSTRIDE = (FBYTES + 127) / 128 * 128 + GUARD;  // ring slot + following guard
+    static constexpr int SSTRIDE = (FBYTES + 127) / 128 * 128 + (CBYTES + 127) / 128 * 128;
+    static constexpr int TAB = (DIV_TABLE_BYTES + 127) / 128 * 128;
+    static constexpr int HEAD = 128 + TAB;             // mbarriers + failure flag, division table
+    static constexpr int RING0 = HEAD + GUARD;         // ring slot r: RING0 + r * RSTRIDE, a guard on each side
+    static constexpr int STAGE0 = RING0 + R * RSTRIDE; // staging buffer d: STAGE0 + d * SSTRIDE (field, codes)
+    static constexpr int SMEM = STAGE0 + D * SSTRIDE;
     static_assert(TJ % 64 == 0, "a pair's interior groups must fill whole warps");
     static_assert(K % 2 == 0 && K >= 2 && K <= HY, "row pairs fuse an even number of half-sweeps");
+    static_assert(R % D == 0 && (R / D) % 2 == 0, "staging parity must repeat with the unrolled march");
     static_assert(4 * HG >= K && 2 * HG <= HJ, "z halo must cover the dependency cone inside the staged ghosts");
-    static_assert(8 * NS <= 120, "mbarriers and the failure flag must fit the head");
+    static_assert(8 * D <= 120, "mbarriers and the failure flag must fit the head");
     static_assert(SMEM <= 227 * 1024, "shared memory per CTA");
+    static_assert(151 * 16 * DIV_COPIES < 65536, "table offsets must fit 16 bits");
+    static_assert(HEAD % 16 == 0 && STAGE0 % 16 == 0, "ring zeroed as float4");
 };
 
 __device__ __forceinline__ f32x2 ld_pair(const float* p) { return *reinterpret_cast<const f32x2*>(p); }
@@ -70,23 +74,19 @@ __device__ __forceinline__ float lo_of(f32x2 v) { float l, h; upk2(v, l, h); ret
 __device__ __forceinline__ float hi_of(f32x2 v) { float l, h; upk2(v, l, h); return h; }
 
 // Neighbour sum of one row's float2 group updating half-row q, in the reference's order
-// (x+1, x-1, y+1, y-1, z+1, z-1). `f` points at the group in half-row q of the row's slot;
-// `zo` is the group of the other half-row (registers). q is a constant after unrolling.
-template <int WJ>
-__device__ __forceinline__ f32x2 rp_sum(int q, f32x2 xp, f32x2 xm, f32x2 zo, const float* f) {
-    const f32x2 yp = ld_pair(f + 2 * WJ);
-    const f32x2 ym = ld_pair(f - 2 * WJ);
+// (x+1, x-1, y+1, y-1, z+1, z-1). `zo` is the group of the other half-row (registers), `e` the
+// z-edge cell of the adjacent group (odd j-1 for q = 0, even j+2 for q = 1). q is a constant
+// after unrolling.
+__device__ __forceinline__ f32x2 rp_sum(int q, f32x2 xp, f32x2 xm, f32x2 yp, f32x2 ym, f32x2 zo, float e) {
     f32x2 s = add2(xp, xm);
     s = add2(s, yp);
     s = add2(s, ym);
     if (q == 0) {
         // even cells j, j+1: z+1 = odd j, j+1 (zo); z-1 = odd j-1 (edge), odd j
-        const float e = f[WJ - 1];
         s = add2(s, zo);
         s = add2(s, pk2(e, lo_of(zo)));
     } else {
         // odd cells j, j+1: z+1 = even j+1, j+2 (edge); z-1 = even j, j+1 (zo)
-        const float e = f[-WJ + 2];
         s = add2(s, pk2(hi_of(zo), e));
         s = add2(s, zo);
     }
@@ -94,9 +94,9 @@ __device__ __forceinline__ f32x2 rp_sum(int q, f32x2 xp, f32x2 xm, f32x2 zo, con
 }
 
 // Quotients sum / neighbour count of one row's lane pair, correctly rounded (Brisebarre, Muller,
-// Raina with the pair table, as update4_binary); `idx` = 9 n_lo + n_hi of the two cells.
-__device__ __forceinline__ f32x2 rp_quotient(f32x2 s, uint32_t idx, const float4* tab) {
-    const float4 t = tab[idx * DIV_COPIES];
+// Raina with the pair table, as update4_binary); `t` = the table entry (-n_lo, -n_hi, RN(1/n_lo),
+// RN(1/n_hi)) of the two cells.
+__device__ __forceinline__ f32x2 rp_quotient(f32x2 s, float4 t) {
     const f32x2 r = pk2(t.z, t.w);
     f32x2 q = mul2(s, r);
     q = fma2(fma2(q, pk2(t.x, t.y), s), r, q);
@@ -112,8 +112,7 @@ __device__ __forceinline__ f32x2 rp_sor(f32x2 c, f32x2 q, float omega) {
 }
 
 // IEEE quotients of one lane pair (the tiny-sum path of update4_binary).
-__device__ __forceinline__ f32x2 rp_tiny(f32x2 s, uint32_t idx, const float4* tab) {
-    const float4 t = tab[idx * DIV_COPIES];
+__device__ __forceinline__ f32x2 rp_tiny(f32x2 s, float4 t) {
     float a, b;
     upk2(s, a, b);
     const float4 q = tiny_quotients(make_float4(a, b, 0.f, 0.f), make_float4(-t.x, -t.y, 1.f, 1.f),
@@ -123,34 +122,6 @@ __device__ __forceinline__ f32x2 rp_tiny(f32x2 s, uint32_t idx, const float4* ta
 
 // |bits - 1| of a lane: +-0 becomes a NaN (skipped by fminf), anything else loses one ulp.
 __device__ __forceinline__ float tiny_key(float v) { return fabsf(__int_as_float(__float_as_int(v) - 1)); }
-
-// One half-sweep of both rows of the pair: P updates half-row qp, Q half-row 1 - qp (qp is a
-// constant after unrolling).
-// `ki` holds the plane's four table indices, one byte each: row P even / odd half-row, then
-// row Q even / odd half-row.
-template <int WJ>
-__device__ __forceinline__ void rp_stage(int qp, f32x2& cP, f32x2 xpP, f32x2 xmP, f32x2 zoP, float* fP,
-                                         f32x2& cQ, f32x2 xpQ, f32x2 xmQ, f32x2 zoQ, float* fQ, uint32_t ki,
-                                         float omega, const float4* tab, bool store) {
-    const int qq = 1 - qp;
-    const uint32_t iP = (ki >> (8 * qp)) & 0xffu, iQ = (ki >> (16 + 8 * qq)) & 0xffu;
-    const f32x2 sP = rp_sum<WJ>(qp, xpP, xmP, zoP, fP);
-    const f32x2 sQ = rp_sum<WJ>(qq, xpQ, xmQ, zoQ, fQ);
-    f32x2 qP = rp_quotient(sP, iP, tab);
-    f32x2 qQ = rp_quotient(sQ, iQ, tab);
-    // 0 < |sum| <= 2^-90: the correction term may underflow; IEEE division instead (never in practice)
-    const float m = fminf(fminf(tiny_key(lo_of(sP)), tiny_key(hi_of(sP))), fminf(tiny_key(lo_of(sQ)), tiny_key(hi_of(sQ))));
-    if (m < 0x1p-90f) {
-        qP = rp_tiny(sP, iP, tab);
-        qQ = rp_tiny(sQ, iQ, tab);
-    }
-    cP = rp_sor(cP, qP, omega);
-    cQ = rp_sor(cQ, qQ, omega);
-    if (store) {
-        st_pair(fP, cP);
-        st_pair(fQ, cQ);
-    }
-}
 
 // Writes one row's two half-row groups of plane `pw` (with periodic ghost copies).
 __device__ __forceinline__ void rp_write_row(const SweepArgs& a, int b, int pw, int y, int j, f32x2 ev, f32x2 od,
@@ -187,24 +158,29 @@ __device__ __forceinline__ void rp_write_row(const SweepArgs& a, int b, int pw, 
     }
 }
 
-template <int TY, int TZ, int K>
+// One CTA's tile (j0 = first staged padded j, y0 = first interior row, volume b, written planes
+// [x0, x1)) for K half-sweeps. RPAR = (x0-chunk start + y0 - K + first colour) & 1: which row
+// of every pair is P (0: the lower one). Shared memory: RowPairShape::SMEM bytes at `smem`.
+//
+// Planes arrive by TMA in D staging buffers, D - 1 ahead; at step t every thread copies its own
+// cells of plane t into ring slot (t - xs) mod R (and its codes into registers), where the K
+// half-sweeps of the following steps read y-neighbours and z-edges and publish their updates.
+// R and D divide the unrolled march, so every slot, buffer and mbarrier phase is a
+// compile-time constant.
+template <int TY, int TZ, int K, int RPAR>
 __device__ __forceinline__ void stream_tile_rp(const CUtensorMap* tmf, const CUtensorMap* tmc, const SweepArgs& a,
                                                int j0, int y0, int b, int x0, int x1, unsigned char* smem) {
     using S = RowPairShape<TY, TZ, K>;
-    constexpr int WJ = S::WJ, WJC = S::WJC, NS = S::NS, D = S::D, R = S::R, NT = S::NT, NP = S::NP;
-    constexpr int FS = S::FSTRIDE / 4;  // floats between slots
+    constexpr int WJ = S::WJ, WJC = S::WJC, D = S::D, R = S::R, NT = S::NT, NP = S::NP;
+    constexpr int RS = S::RSTRIDE / 4, SS = S::SSTRIDE / 4;  // floats between ring slots / staging buffers
     uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
     int* s_fail = reinterpret_cast<int*>(smem + 120);
     float4* tab_all = reinterpret_cast<float4*>(smem + 128);
-    const float4* tab = division_copy(tab_all);
-    float* const F0 = reinterpret_cast<float*>(smem + S::FIELD0);
-    unsigned char* const C0 = smem + S::CODE0;
 
     const Geo& g = a.g;
     const int tid = threadIdx.x;
     const int warp = tid >> 5, lane = tid & 31;
     const int NX = g.NX;
-    const int c0 = a.first_colour;
 
     // thread -> (pair k, float2 group gi); halo lanes beyond the halo threads repeat them (dup)
     int k, gi;
@@ -224,139 +200,199 @@ __device__ __forceinline__ void stream_tile_rp(const CUtensorMap* tmf, const CUt
         gi = e < S::HG ? e : S::GM + e;
     }
     const int jj = HJ - 2 * S::HG + 2 * gi;  // staged float index of the group's first cell
+    // float offset of the pair's lower row (half-row 0) at the group; the upper row is + 2 WJ
+    const int base = 4 * k * WJ + jj;
+    float* const ring = reinterpret_cast<float*>(smem + S::RING0) + base;
+    const float* const stage_f = reinterpret_cast<const float*>(smem + S::STAGE0) + base;
+    const unsigned char* const stage_c = smem + S::STAGE0 + S::FBYTES + 4 * k * WJC + jj;
+    // byte offset of this thread's copy of the division table, added to 16 * DIV_COPIES * index
+    const uint32_t copy_off = 16u * (uint32_t)(tid & (DIV_COPIES - 1));
 
     if (tid == 0) {
-        for (int s = 0; s < NS; ++s) mbar_init(&bar[s], 1);
+        for (int d = 0; d < D; ++d) mbar_init(&bar[d], 1);
         fence_mbar_init();
         *s_fail = 0;
     }
     fill_division_table(tab_all, tid, NT);
-    // zero guards: [HEAD, FIELD0) before slot 0, and from the end of each slot's field to the
-    // next slot (rows -1 and ROWS of every slot read zeros)
-    for (int s = -1; s < NS; ++s) {
-        const int lo = s < 0 ? S::HEAD : S::FIELD0 + s * S::FSTRIDE + S::FBYTES;
-        const int hi = S::FIELD0 + (s + 1) * S::FSTRIDE;
-        float* gp = reinterpret_cast<float*>(smem + lo);
-        for (int i = tid; i < (hi - lo) / 4; i += NT) gp[i] = 0.0f;
+    // zero the guard before ring slot 0 and the whole ring with its guards: rows -1 and ROWS
+    // read zeros, and so do the staged ghost cells no thread owns (positions < HJ - 2 HG and
+    // >= WJ - HJ + 2 HG of every half-row, read as z-edges by the halo groups), which would
+    // otherwise hold whatever the shared memory held before
+    {
+        float4* z = reinterpret_cast<float4*>(smem + S::HEAD);
+        for (int i = tid; i < (S::STAGE0 - S::HEAD) / 16; i += NT) z[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     __syncthreads();
 
     const int xs = x0 > K ? x0 - K : 0;
     const int xe = x1 + K < NX ? x1 + K : NX;
     const int row0 = 2 * (y0 + HY - K);
-    auto issue = [&](int x) {
-        const int s = (int)((unsigned)(x - xs) % NS);
-        mbar_arrive_expect_tx(&bar[s], S::FBYTES + S::CBYTES);
-        tma_load_3d(F0 + s * FS, tmf, &bar[s], j0, row0, b * NX + x);
-        tma_load_3d(C0 + s * S::CSTRIDE, tmc, &bar[s], j0, row0, b * NX + x);
+    auto issue = [&](int x, int d) {
+        mbar_arrive_expect_tx(&bar[d], S::FBYTES + S::CBYTES);
+        float* dst = reinterpret_cast<float*>(smem + S::STAGE0 + d * S::SSTRIDE);
+        tma_load_3d(dst, tmf, &bar[d], j0, row0, b * NX + x);
+        tma_load_3d(reinterpret_cast<unsigned char*>(dst) + S::FBYTES, tmc, &bar[d], j0, row0, b * NX + x);
     };
     if (tid == 0)
-        for (int x = xs; x < xs + D && x < xe; ++x) issue(x);
+        for (int x = xs; x < xs + D - 1 && x < xe; ++x) issue(x, x - xs);
 
-    // rows of the pair: P has (xs + y + c0) even
-    const int rp = (xs + y0 - K + c0) & 1;
-    const int rP = 2 * k + rp, rQ = 2 * k + 1 - rp;
-    const int yP = y0 - K + rP, yQ = y0 - K + rQ;
-    const int offP = 2 * rP * WJ + jj, offQ = 2 * rQ * WJ + jj;     // half-row 0 of each row (floats)
-    const int coP = 2 * rP * WJC + jj, coQ = 2 * rQ * WJC + jj;     // code bytes
-    // bit s: the pair takes part in half-sweep s (a row of it lies in [s, ROWS - s)); the halo warp
-    // takes part in every half-sweep
+    // rows of the pair: P is the lower row when RPAR == 0
+    constexpr int LP = RPAR ? 2 * WJ : 0, LQ = RPAR ? 0 : 2 * WJ;    // float offsets of rows P, Q
+    constexpr int CP = RPAR ? 2 * WJC : 0, CQ = RPAR ? 0 : 2 * WJC;  // their code byte offsets
+    const int yL = y0 - K + 2 * k;  // interior y of the lower row
+    const int yP = yL + (RPAR ? 1 : 0), yQ = yL + (RPAR ? 0 : 1);
+    // bit s: the pair takes part in half-sweep s (a row of it lies in [s, ROWS - s)); the halo
+    // warp takes part in every half-sweep
     uint32_t stage_mask = 0;
 #pragma unroll
     for (int s = 1; s <= K; ++s)
         stage_mask |= (halo || (2 * k + 1 >= s && 2 * k < S::ROWS - s)) ? (1u << s) : 0u;
-    const bool wP = !halo && rP >= K && rP < K + TY && yP < g.NY;
-    const bool wQ = !halo && rQ >= K && rQ < K + TY && yQ < g.NY;
+    const bool wP = !halo && (2 * k + (RPAR ? 1 : 0)) >= K && (2 * k + (RPAR ? 1 : 0)) < K + TY && yP < g.NY;
+    const bool wQ = !halo && (2 * k + (RPAR ? 0 : 1)) >= K && (2 * k + (RPAR ? 0 : 1)) < K + TY && yQ < g.NY;
     const int jglob = j0 + jj - HJ;  // interior index of the group's first cell
     const bool py = a.periodic & TF_PERIODIC_Y, pz = a.periodic & TF_PERIODIC_Z;
     const float omega = a.omega;
 
-    // ring by relative colour: P0/P1 (row P), Q0/Q1 (row Q); KI: the division-table indices of
-    // the plane's four half-row groups (bytes: P even, P odd, Q even, Q odd)
+    // ring by relative colour: P0/P1 (row P), Q0/Q1 (row Q); TP/TQ: byte offsets of the division
+    // table entries of the row's even (low 16 bits) and odd (high 16 bits) half-row groups
     f32x2 P0[R], P1[R], Q0[R], Q1[R];
-    uint32_t KI[R];
+    uint32_t TP[R], TQ[R];
     const f32x2 glo = pk2(a.glo, a.glo), ghi = pk2(a.ghi, a.ghi);
 #pragma unroll
     for (int r = 0; r < R; ++r) {
         P0[r] = P1[r] = Q0[r] = Q1[r] = glo;
-        KI[r] = 0u;
+        TP[r] = TQ[r] = 0u;
     }
+    const unsigned char* const tab_base = smem + 128;
 
     const int total = xe == NX ? NX + K : xe;
-    for (int t0 = xs; t0 < total; t0 += R) {
+    // One block of R steps starting at t0 (t0 - xs a multiple of R). CHECKED: any block; else a
+    // block in the steady state (t0 >= x0 + K and t0 + R <= xe), where every step loads its
+    // plane, runs all K half-sweeps and writes back, so the range checks drop out.
+    auto block = [&](auto checked, int t0) -> bool {
+        constexpr bool CK = decltype(checked)::value;
 #pragma unroll
         for (int i = 0; i < R; ++i) {
             const int t = t0 + i;
-            if (t < total) {
-                if (tid == 0 && t + D < xe) issue(t + D);
-                if (t < xe) {
-                    const int slot = (int)((unsigned)(t - xs) % NS);
-                    if (!mbar_wait_bounded(&bar[slot], ((unsigned)(t - xs) / NS) & 1)) *s_fail = 1;
-                    const float* Fs = F0 + slot * FS;
-                    const unsigned char* Cs = C0 + slot * S::CSTRIDE;
-                    const f32x2 eP = ld_pair(Fs + offP), oP = ld_pair(Fs + offP + WJ);
-                    const f32x2 eQ = ld_pair(Fs + offQ), oQ = ld_pair(Fs + offQ + WJ);
-                    // 9 n_lo + n_hi per half-row group, counts masked to 4 bits (index <= 150:
-                    // inside the CTA's shared memory whatever the code bytes hold)
-                    const uint32_t cP = (ld_u16(Cs + coP) | (ld_u16(Cs + coP + WJC) << 16)) & 0x0f0f0f0fu;
-                    const uint32_t cQ = (ld_u16(Cs + coQ) | (ld_u16(Cs + coQ + WJC) << 16)) & 0x0f0f0f0fu;
-                    KI[i] = (uint32_t)__dp4a((int)cP, 0x0109, 0) | ((uint32_t)__dp4a((int)cP, 0x01090000, 0) << 8) |
-                            ((uint32_t)__dp4a((int)cQ, 0x0109, 0) << 16) |
-                            ((uint32_t)__dp4a((int)cQ, 0x01090000, 0) << 24);
-                    // relative colour 0 of row P is its even half-row at even i; row Q the opposite
-                    if ((i & 1) == 0) {
-                        P0[i] = eP; P1[i] = oP; Q0[i] = oQ; Q1[i] = eQ;
-                    } else {
-                        P0[i] = oP; P1[i] = eP; Q0[i] = eQ; Q1[i] = oQ;
-                    }
-                } else if (t == NX) {
-                    P0[i] = P1[i] = Q0[i] = Q1[i] = ghi;
+            if (CK && t >= total) continue;
+            if (tid == 0 && t + D - 1 < xe) issue(t + D - 1, (i + D - 1) % D);
+            if (!CK || t < xe) {
+                const int d = i % D;
+                if (!mbar_wait_bounded(&bar[d], (i / D) & 1)) *s_fail = 1;
+                const float* fs = stage_f + d * SS;
+                const unsigned char* cs = stage_c + d * S::SSTRIDE;
+                float* fr = ring + i * RS;
+                const f32x2 eP = ld_pair(fs + LP), oP = ld_pair(fs + LP + WJ);
+                const f32x2 eQ = ld_pair(fs + LQ), oQ = ld_pair(fs + LQ + WJ);
+                st_pair(fr + LP, eP);
+                st_pair(fr + LP + WJ, oP);
+                st_pair(fr + LQ, eQ);
+                st_pair(fr + LQ + WJ, oQ);
+                // counts masked to 4 bits: table offsets stay inside shared memory whatever
+                // the code bytes hold
+                const uint32_t cP = (ld_u16(cs + CP) | (ld_u16(cs + CP + WJC) << 16)) & 0x0f0f0f0fu;
+                const uint32_t cQ = (ld_u16(cs + CQ) | (ld_u16(cs + CQ + WJC) << 16)) & 0x0f0f0f0fu;
+                constexpr uint32_t ENT = 16u * DIV_COPIES;  // bytes per table entry (all copies)
+                TP[i] = ((uint32_t)__dp4a((int)cP, 0x0109, 0) * ENT + copy_off) |
+                        (((uint32_t)__dp4a((int)cP, 0x01090000, 0) * ENT + copy_off) << 16);
+                TQ[i] = ((uint32_t)__dp4a((int)cQ, 0x0109, 0) * ENT + copy_off) |
+                        (((uint32_t)__dp4a((int)cQ, 0x01090000, 0) * ENT + copy_off) << 16);
+                // relative colour 0 of row P is its even half-row at even i; row Q the opposite
+                if ((i & 1) == 0) {
+                    P0[i] = eP; P1[i] = oP; Q0[i] = oQ; Q1[i] = eQ;
+                } else {
+                    P0[i] = oP; P1[i] = eP; Q0[i] = eQ; Q1[i] = oQ;
                 }
-                const int qp = (i + 1) & 1;  // half-row updated by row P in this step
+            } else if (t == NX) {
+                P0[i] = P1[i] = Q0[i] = Q1[i] = ghi;
+            }
+            const int qp = (i + 1) & 1;  // half-row updated by row P in this step
+            const int qq = 1 - qp;
 #pragma unroll
-                for (int s = 1; s <= K; ++s) {
-                    const int p = t - s;
-                    const int ip = (i - s + 2 * R) % R;
-                    const int ipn = (i - s + 1 + 2 * R) % R;
-                    const int ipp = (i - s - 1 + 2 * R) % R;
-                    if (p >= xs && p < NX && (stage_mask & (1u << s))) {
-                        float* Fp = F0 + (int)((unsigned)(p - xs) % NS) * FS;
-                        if (((s - 1) & 1) == 0) {
-                            rp_stage<WJ>(qp, P0[ip], P1[ipn], P1[ipp], P1[ip], Fp + offP + qp * WJ,
-                                         Q0[ip], Q1[ipn], Q1[ipp], Q1[ip], Fp + offQ + (1 - qp) * WJ, KI[ip],
-                                         omega, tab, !dup);
-                        } else {
-                            rp_stage<WJ>(qp, P1[ip], P0[ipn], P0[ipp], P0[ip], Fp + offP + qp * WJ,
-                                         Q1[ip], Q0[ipn], Q0[ipp], Q0[ip], Fp + offQ + (1 - qp) * WJ, KI[ip],
-                                         omega, tab, !dup);
-                        }
+            for (int s = 1; s <= K; ++s) {
+                const int p = t - s;
+                const int ip = (i - s + 2 * R) % R;
+                const int ipn = (i - s + 1 + 2 * R) % R;
+                const int ipp = (i - s - 1 + 2 * R) % R;
+                if ((!CK || (p >= xs && p < NX)) && __any_sync(0xffffffffu, (stage_mask >> s) & 1u)) {
+                    float* fr = ring + ip * RS;
+                    const int rc = (s - 1) & 1;
+                    f32x2& cP = rc ? P1[ip] : P0[ip];
+                    f32x2& cQ = rc ? Q1[ip] : Q0[ip];
+                    const f32x2 oP = rc ? P0[ip] : P1[ip], oQ = rc ? Q0[ip] : Q1[ip];
+                    const f32x2 xpP = rc ? P0[ipn] : P1[ipn], xmP = rc ? P0[ipp] : P1[ipp];
+                    const f32x2 xpQ = rc ? Q0[ipn] : Q1[ipn], xmQ = rc ? Q0[ipp] : Q1[ipp];
+                    // y-neighbours: the pair's other row from registers (its cells in the
+                    // updated half-row have the other colour), the far side from the slot
+                    f32x2 ypP, ymP, ypQ, ymQ;
+                    if (RPAR == 0) {  // P lower, Q upper
+                        ypP = oQ;
+                        ymP = ld_pair(fr + LP - 2 * WJ + qp * WJ);
+                        ypQ = ld_pair(fr + LQ + 2 * WJ + qq * WJ);
+                        ymQ = oP;
+                    } else {  // P upper, Q lower
+                        ypP = ld_pair(fr + LP + 2 * WJ + qp * WJ);
+                        ymP = oQ;
+                        ypQ = oP;
+                        ymQ = ld_pair(fr + LQ - 2 * WJ + qq * WJ);
                     }
-                }
-                // write back plane t-K from registers: even half-row of P is relative colour 0 at even i
-                const int pw = t - K;
-                const int iw = (i - K + 2 * R) % R;
-                if (pw >= x0 && pw < x1) {
-                    if (wP) {
-                        if ((i & 1) == 0) rp_write_row(a, b, pw, yP, jglob, P0[iw], P1[iw], py, pz);
-                        else rp_write_row(a, b, pw, yP, jglob, P1[iw], P0[iw], py, pz);
+                    // z-edges: odd j-1 for an even half-row, even j+2 for an odd one
+                    const float eP = qp == 0 ? fr[LP + WJ - 1] : fr[LP + 2];
+                    const float eQ = qq == 0 ? fr[LQ + WJ - 1] : fr[LQ + 2];
+                    const f32x2 sP = rp_sum(qp, xpP, xmP, ypP, ymP, oP, eP);
+                    const f32x2 sQ = rp_sum(qq, xpQ, xmQ, ypQ, ymQ, oQ, eQ);
+                    const uint32_t offP = qp ? (TP[ip] >> 16) : (TP[ip] & 0xffffu);
+                    const uint32_t offQ = qq ? (TQ[ip] >> 16) : (TQ[ip] & 0xffffu);
+                    const float4 tP = *reinterpret_cast<const float4*>(tab_base + offP);
+                    const float4 tQ = *reinterpret_cast<const float4*>(tab_base + offQ);
+                    f32x2 quP = rp_quotient(sP, tP);
+                    f32x2 quQ = rp_quotient(sQ, tQ);
+                    // 0 < |sum| <= 2^-90: the correction term may underflow; IEEE division
+                    // for the whole warp instead (never in practice)
+                    const float m = fminf(fminf(tiny_key(lo_of(sP)), tiny_key(hi_of(sP))),
+                                          fminf(tiny_key(lo_of(sQ)), tiny_key(hi_of(sQ))));
+                    if (__any_sync(0xffffffffu, m < 0x1p-90f)) {
+                        quP = rp_tiny(sP, tP);
+                        quQ = rp_tiny(sQ, tQ);
                     }
-                    if (wQ) {
-                        if ((i & 1) == 0) rp_write_row(a, b, pw, yQ, jglob, Q1[iw], Q0[iw], py, pz);
-                        else rp_write_row(a, b, pw, yQ, jglob, Q0[iw], Q1[iw], py, pz);
+                    cP = rp_sor(cP, quP, omega);
+                    cQ = rp_sor(cQ, quQ, omega);
+                    if (!dup) {
+                        st_pair(fr + LP + qp * WJ, cP);
+                        st_pair(fr + LQ + qq * WJ, cQ);
                     }
-                }
-                fence_proxy_async_smem();
-                __syncthreads();
-                if (*s_fail) {
-                    if (tid == 0) {
-                        for (int x = t + 1; x < t + 1 + D && x < xe; ++x)
-                            mbar_wait_bounded(&bar[(x - xs) % NS], ((x - xs) / NS) & 1);
-                        if (a.err) atomicExch(a.err, TF_ERR_TIMEOUT);
-                    }
-                    return;
                 }
             }
+            // write back plane t-K from registers: even half-row of P is relative colour 0 at even i
+            const int pw = t - K;
+            const int iw = (i - K + 2 * R) % R;
+            if (!CK || (pw >= x0 && pw < x1)) {
+                if (wP) {
+                    if ((i & 1) == 0) rp_write_row(a, b, pw, yP, jglob, P0[iw], P1[iw], py, pz);
+                    else rp_write_row(a, b, pw, yP, jglob, P1[iw], P0[iw], py, pz);
+                }
+                if (wQ) {
+                    if ((i & 1) == 0) rp_write_row(a, b, pw, yQ, jglob, Q1[iw], Q0[iw], py, pz);
+                    else rp_write_row(a, b, pw, yQ, jglob, Q0[iw], Q1[iw], py, pz);
+                }
+            }
+            // the staging buffer read above is refilled by TMA after the barrier
+            fence_proxy_async_smem();
+            __syncthreads();
+            if (*s_fail) {
+                if (tid == 0) {
+                    for (int x = t + 1; x < t + D && x < xe; ++x)
+                        mbar_wait_bounded(&bar[(x - xs) % D], ((x - xs) / D) & 1);
+                    if (a.err) atomicExch(a.err, TF_ERR_TIMEOUT);
+                }
+                return false;
+            }
         }
+        return true;
+    };
+    for (int t0 = xs; t0 < total; t0 += R) {
+        const bool ok = (t0 >= x0 + K && t0 + R <= xe) ? block(std::false_type{}, t0) : block(std::true_type{}, t0);
+        if (!ok) return;
     }
 }
 
@@ -367,7 +403,13 @@ __global__ void __launch_bounds__(RowPairShape<TY, TZ, K>::NT, 1)
     extern __shared__ __align__(128) unsigned char smem[];
     const int b = blockIdx.z / a.x_chunks, c = blockIdx.z - b * a.x_chunks;
     const int x0 = (int)((long long)c * a.g.NX / a.x_chunks), x1 = (int)((long long)(c + 1) * a.g.NX / a.x_chunks);
-    stream_tile_rp<TY, TZ, K>(&tmf, &tmc, a, blockIdx.x * (TZ / 2), blockIdx.y * TY, b, x0, x1, smem);
+    const int xs = x0 > K ? x0 - K : 0;
+    const int y0 = blockIdx.y * TY;
+    // CTA-uniform: which row of each pair has (xs + y + first colour) even
+    if (((xs + y0 - K + a.first_colour) & 1) == 0)
+        stream_tile_rp<TY, TZ, K, 0>(&tmf, &tmc, a, blockIdx.x * (TZ / 2), y0, b, x0, x1, smem);
+    else
+        stream_tile_rp<TY, TZ, K, 1>(&tmf, &tmc, a, blockIdx.x * (TZ / 2), y0, b, x0, x1, smem);
 }
 
 template <int TY, int TZ, int K>
