@@ -353,41 +353,6 @@ class SORSolver:
                 out[:, :, :, -1] = out[:, :, :, 1]
         return out
 
-    # ------------------------------------------------------------------ operator tensors
-    # The reference keeps its operator as tensors (taufactor.py:43-67): the divisor `factor`
-    # [B,Nx,Ny,Nz] (inf where a voxel is frozen), the over-relaxation chequerboards `cb` and,
-    # for the multiphase solvers, the face diffusivities D_x, D_y, D_z. The kernels here never
-    # form them; they are built on first access, on the device, with the reference's formulas.
-    @property
-    def cb(self):
-        """[omega * cb, omega * (1 - cb)] with cb = 1 where (x + y + z) is even (taufactor.py:218-225)."""
-        cached = getattr(self, "_cb_tensors", None)
-        if cached is None:
-            dev = self.device
-            par = (torch.arange(self.Nx, device=dev)[:, None, None] + torch.arange(self.Ny, device=dev)[None, :, None]
-                   + torch.arange(self.Nz, device=dev)[None, None, :]) % 2
-            w = torch.tensor(self.omega, dtype=torch.float64, device=dev)
-            zero = torch.zeros((), dtype=torch.float64, device=dev)
-            cached = [torch.where(par == 0, w, zero).to(self.precision), torch.where(par == 1, w, zero).to(self.precision)]
-            self._cb_tensors = cached
-        return cached
-
-    @property
-    def factor(self) -> torch.Tensor:
-        """The divisor of the update per voxel, [B,Nx,Ny,Nz] (inf = frozen), as the reference's
-        init_conductive_neighbours returns it for this solver class."""
-        cached = getattr(self, "_factor_tensor", None)
-        if cached is None:
-            cached = self._build_factor()
-            self._factor_tensor = cached
-        return cached
-
-    def _labels_tensor(self) -> torch.Tensor:
-        return torch.from_numpy(np.ascontiguousarray(self.cpu_img)).to(self.device).to(self.precision)
-
-    def _build_factor(self) -> torch.Tensor:
-        raise NotImplementedError(f"{type(self).__name__} has no divisor tensor")
-
     @field.setter
     def field(self, value: torch.Tensor):
         shape = (self.batch_size, self.Nx + 2, self.Ny + 2, self.Nz + 2)
@@ -566,6 +531,42 @@ class ThroughTransportSolver(SORSolver):
         """taufactor.py:293-331 on float64 layer means read back from the device."""
         self.flux_1d, c_x = self._layer_means()
         return layer_metrics(self, self.flux_1d, c_x)
+
+    # ------------------------------------------------------------------ operator tensors
+    # The reference keeps its operator as tensors (taufactor.py:43-67): the divisor `factor`
+    # [B,Nx,Ny,Nz] (inf where a voxel is frozen), the over-relaxation chequerboards `cb` and,
+    # for the multiphase solvers, the face diffusivities D_x, D_y, D_z. The kernels here never
+    # form them; they are built on first access, on the device, with the reference's formulas.
+    @property
+    def cb(self):
+        """[omega * cb, omega * (1 - cb)] with cb = 1 where (x + y + z) is even (taufactor.py:218-225)."""
+        cached = getattr(self, "_cb_tensors", None)
+        if cached is None:
+            dev = self.device
+            par = (torch.arange(self.Nx, device=dev)[:, None, None] + torch.arange(self.Ny, device=dev)[None, :, None]
+                   + torch.arange(self.Nz, device=dev)[None, None, :]) % 2
+            w = torch.tensor(self.omega, dtype=torch.float64, device=dev)
+            zero = torch.zeros((), dtype=torch.float64, device=dev)
+            cached = [torch.where(par == 0, w, zero).to(self.precision), torch.where(par == 1, w, zero).to(self.precision)]
+            self._cb_tensors = cached
+        return cached
+
+    @property
+    def factor(self) -> torch.Tensor:
+        """The divisor of the update per voxel, [B,Nx,Ny,Nz] (inf = frozen), as the reference's
+        init_conductive_neighbours returns it for this solver class."""
+        cached = getattr(self, "_factor_tensor", None)
+        if cached is None:
+            cached = self._build_factor()
+            self._factor_tensor = cached
+        return cached
+
+    def _labels_tensor(self) -> torch.Tensor:
+        return torch.from_numpy(np.ascontiguousarray(self.cpu_img)).to(self.device).to(self.precision)
+
+    def _build_factor(self) -> torch.Tensor:
+        raise NotImplementedError(f"{type(self).__name__} has no divisor tensor")
+
 
 
 def layer_metrics(s, flux_1d: np.ndarray, c_x_raw: np.ndarray):
