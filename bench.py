@@ -740,11 +740,12 @@ def impedance_throughput(dev, side=256, nyq_side=64, cpu_half_sweeps=4):
     r = b.solve_frequencies()
     torch.cuda.synchronize()
     t_bat = time.perf_counter() - t3
-    # frequencies that both runs converged with a finite, non-zero tau (a NaN field ends a
-    # frequency with tau = inf and its impedance left at 0)
-    seq_tau = np.array([float(np.asarray(v)[0]) for v in a.taus])
-    both = (np.array(a.converged_freq) & r["converged"] & np.isfinite(seq_tau) & (seq_tau != 0)
-            & np.isfinite(r["tau"]) & (r["tau"] != 0))
+    # frequencies that both runs converged with a finite, non-zero impedance (a NaN field ends a
+    # frequency with its impedance left at 0; in Nyquist mode the sequential run keeps no tau)
+    imp_a = np.array([complex(z) for z in a.impedance])
+    imp_b = np.asarray(r["impedance"])
+    both = (np.array(a.converged_freq, dtype=bool) & np.asarray(r["converged"], dtype=bool)
+            & np.isfinite(imp_a) & (imp_a != 0) & np.isfinite(imp_b) & (imp_b != 0))
     agree = [abs(complex(a.impedance[k]) - r["impedance"][k]) / abs(r["impedance"][k]) for k in np.flatnonzero(both)]
     return {"workload": f"ImpedanceSolver {side}^3 pore volume (porosity 0.45, sigma 2, rng 5000; isolated pores inert)",
             "dtype": "complex128", "half_sweeps": int(s.sum_iter), "converged_freq": s.converged_freq,
