@@ -156,12 +156,15 @@ int tf_axpy_f64(const tf_geom* g, double* field64_dev, const float* e_dev, void*
 /* float64 residual r = b - A c of the operator the reference's iteration converges to
  * (A c = d c - weighted in-volume neighbour sum, b = Dirichlet ghost terms; taufactor.py:95-103,
  * :176-181, :598-613). Writes r as float32 into rhs_dev (split layout, periodic ghost copies)
- * and per-plane float64 sums of r^2 and b^2 into r2_sum_dev / b2_sum_dev [batch][nx]. */
+ * and per-plane float64 sums of r^2 and b^2 into r2_sum_dev / b2_sum_dev [batch][nx].
+ * TF_KIND_ELECTRODE: d = the sweep's float32 nn + nr * k_0 (taufactor.py:47-55), b = the inlet
+ * ghost term; the closed outlet adds nothing. */
 int tf_residual_f64(const tf_geom* g, const tf_operator* op, const double* field64_dev,
                     const uint8_t* code_dev, float* rhs_dev, double* r2_sum_dev, double* b2_sum_dev,
                     void* stream);
 
-/* tf_layer_sums on a float64 field (differences and products in float64). */
+/* tf_layer_sums on a float64 field (differences and products in float64); for
+ * TF_KIND_ELECTRODE the [batch][nx] plane fluxes of ElectrodeSolver, as tf_layer_sums. */
 int tf_layer_sums_f64(const tf_geom* g, const tf_operator* op, const double* field64_dev,
                       const uint8_t* code_dev, double* flux_sum_dev, double* c_sum_dev, void* stream);
 

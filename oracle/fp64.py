@@ -252,3 +252,55 @@ def adjoint_gradient_fp64(o: OracleSolve, rtol: float = 1e-12, coefficients: str
                 g[sw] += djf * dface(k[sw], k[su])
         grads[b] = g
     return grads
+
+
+def electrode_fp64(o: OracleSolve, rtol: float = 1e-12):
+    """FP64 solution of the ElectrodeSolver operator (electrode.py:13-157, taufactor.py:40-55):
+    for conductive voxels d c - (sum of conductive face neighbours) = b, d = the float32 factor
+    nn + nr k_0 of the sweeps, b = the inlet ghost value 2 left_bc on x = 0 (the outlet is closed);
+    y/z wrap for the periodic kind. Sets o.field to the padded float64 solution and returns
+    (tau, k_x) from electrode_metrics on float64 layer means. Voxels of clusters that touch
+    neither the inlet nor the reactive phase (singular blocks) keep the values o.field had."""
+    B, X, Y, Z = o.batch_size, o.Nx, o.Ny, o.Nz
+    field = o.field.astype(np.float64)
+    idx = np.arange(X * Y * Z).reshape(X, Y, Z)
+    for b in range(B):
+        fac = o.factor[b].astype(np.float64)
+        cond = (o.mask[b] > 0) & np.isfinite(fac)
+        rows, cols = [], []
+        for ax in range(3):
+            nb = np.roll(idx, -1, ax)
+            ok = cond & np.roll(cond, -1, ax)
+            if ax == 0 or not o.periodic:  # no wrap across a closed face
+                sl = [slice(None)] * 3
+                sl[ax] = -1
+                ok[tuple(sl)] = False
+            u, v = idx[ok], nb[ok]
+            rows += [u, v]
+            cols += [v, u]
+        n = X * Y * Z
+        off = sp.csr_matrix((np.ones(sum(len(r) for r in rows)), (np.concatenate(rows), np.concatenate(cols))),
+                            shape=(n, n))
+        rhs = np.zeros(n)
+        rhs[idx[0][cond[0]]] = 2 * o.left_bc
+        diag = np.where(cond, fac, 0.0).ravel()
+        # keep clusters with an inlet face or a reaction term (non-singular blocks)
+        ncomp, comp = connected_components(off, directed=False)
+        anchored = np.zeros(ncomp, dtype=bool)
+        anchored[comp[idx[0][cond[0]]]] = True
+        nn = np.asarray(off.sum(axis=1)).ravel()
+        reactive = cond.ravel() & (diag > nn + 2 * (np.arange(n) < Y * Z) * cond.ravel())
+        anchored[comp[reactive]] = True
+        keep = cond.ravel() & anchored[comp]
+        k = np.nonzero(keep)[0]
+        A = (sp.diags(diag) - off).tocsr()[k][:, k]
+        sol, info = cg(A, rhs[k], rtol=rtol, atol=0.0, maxiter=200000, M=sp.diags(1.0 / A.diagonal()))
+        if info != 0:
+            raise RuntimeError(f"electrode FP64 CG did not reach rtol={rtol}")
+        f = field[b, 1:-1, 1:-1, 1:-1].ravel().copy()
+        f[k] = sol
+        field[b, 1:-1, 1:-1, 1:-1] = f.reshape(X, Y, Z)
+    o.field = field
+    o.c_x = 0
+    tau, _ = o.electrode_metrics(np.float64)
+    return tau, o.k_x

@@ -308,22 +308,23 @@ class OracleSolve:
         self.old_tau = 0
         self.tau = self.tau_x = self.D_eff = None
 
-    def electrode_layer_means(self):
+    def electrode_layer_means(self, dtype=F32):
         """float64 per-layer means of ElectrodeSolver's fluxes [B,Nx] and of the field [B,Nx]
         (electrode.py:65, :70-74): plane 0 (left_bc - c)/0.5, plane x > 0 c[x-1] - c[x], 0 where
-        c or c[x-1] is 0."""
+        c or c[x-1] is 0. The fluxes are formed in float32 like the reference's, or in float64
+        (dtype=np.float64) for a float64 field."""
         f = self.field
         c = f[:, 1:-1, 1:-1, 1:-1]
         cm = f[:, :-2, 1:-1, 1:-1]
-        fl = (-c + cm).astype(F32)
-        fl[:, 0] = (F32(self.left_bc) - c[:, 0]) / F32(0.5)
+        fl = (-c + cm).astype(dtype)
+        fl[:, 0] = (dtype(self.left_bc) - c[:, 0]) / dtype(0.5)
         fl[c == 0] = 0
         fl[cm == 0] = 0
         return fl.astype(np.float64).mean(axis=(2, 3)), c.astype(np.float64).mean(axis=(2, 3))
 
-    def electrode_metrics(self):
+    def electrode_metrics(self, dtype=F32):
         """electrode.py:64-103 on the float64 layer means."""
-        fluxes, c_raw = self.electrode_layer_means()
+        fluxes, c_raw = self.electrode_layer_means(dtype)
         vol_x = self.vol_x
         c_x = np.divide(c_raw, vol_x, out=np.zeros(c_raw.shape), where=vol_x != 0)
         rel = np.max(np.abs(c_x - self.c_x), axis=1)

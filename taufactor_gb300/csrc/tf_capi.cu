@@ -171,7 +171,6 @@ int tf_advance(const tf_geom* g, const tf_operator* op, float* field_a_dev, floa
 int tf_advance_rhs(const tf_geom* g, const tf_operator* op, float* field_a_dev, float* field_b_dev,
                    const uint8_t* code_dev, const float* rhs_dev, int first_colour, int n_half, int32_t* err_dev,
                    int* result_in_b, void* stream) {
-    if (op && op->kind == TF_KIND_ELECTRODE) return TF_ERR_UNSUPPORTED;  // through-transport only
     if (!rhs_dev || (reinterpret_cast<uintptr_t>(rhs_dev) & 15)) return TF_ERR_ARG;
     return advance_impl(g, op, field_a_dev, field_b_dev, code_dev, rhs_dev, first_colour, n_half, err_dev,
                         result_in_b, stream);
@@ -195,7 +194,6 @@ int tf_axpy_f64(const tf_geom* g, double* field64_dev, const float* e_dev, void*
 
 int tf_residual_f64(const tf_geom* g, const tf_operator* op, const double* field64_dev, const uint8_t* code_dev,
                     float* rhs_dev, double* r2_sum_dev, double* b2_sum_dev, void* stream) {
-    if (op && op->kind == TF_KIND_ELECTRODE) return TF_ERR_UNSUPPORTED;  // through-transport only
     if (!valid_geom(g) || !valid_op(op) || !field64_dev || !code_dev || !rhs_dev || !r2_sum_dev || !b2_sum_dev)
         return TF_ERR_ARG;
     return residual(*g, *op, field64_dev, code_dev, rhs_dev, r2_sum_dev, b2_sum_dev, (cudaStream_t)stream);
@@ -203,7 +201,6 @@ int tf_residual_f64(const tf_geom* g, const tf_operator* op, const double* field
 
 int tf_layer_sums_f64(const tf_geom* g, const tf_operator* op, const double* field64_dev, const uint8_t* code_dev,
                       double* flux_sum_dev, double* c_sum_dev, void* stream) {
-    if (op && op->kind == TF_KIND_ELECTRODE) return TF_ERR_UNSUPPORTED;  // through-transport only
     if (!valid_geom(g) || !valid_op(op) || !field64_dev || !code_dev || !c_sum_dev || (g->nx > 1 && !flux_sum_dev))
         return TF_ERR_ARG;
     return layer_sums_f64(*g, *op, field64_dev, code_dev, flux_sum_dev, c_sum_dev, (cudaStream_t)stream);

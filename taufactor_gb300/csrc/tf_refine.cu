@@ -140,7 +140,19 @@ __global__ void __launch_bounds__(256) k_residual(const double* __restrict__ c64
                 res = rhs - ((double)div * c - s);
             }
         } else {
-            const double d = (double)lut[cd];
+            // divisor: the table entry of the code; for the electrode kind the sweep's float32
+            // nn + nr * k_0 (code 1 + nn + 8 nr, k_0 of volume b in the table; taufactor.py:47-55)
+            double d;
+            if (op.kind == TF_KIND_ELECTRODE) {
+                d = 1e300;
+                if (cd != 0) {
+                    const int m = cd - 1;
+                    const float df = __fadd_rn(static_cast<float>(m & 7), __fmul_rn(static_cast<float>(m >> 3), lut[b & 255]));
+                    if (df != 0.0f) d = (double)df;
+                }
+            } else {
+                d = (double)lut[cd];
+            }
             if (d < 1e30) {  // conductive, non-isolated
                 const double ky = op.kind == TF_KIND_ANISOTROPIC ? (double)op.ky : 1.0;
                 const double kz = op.kind == TF_KIND_ANISOTROPIC ? (double)op.kz : 1.0;
@@ -189,7 +201,14 @@ __global__ void __launch_bounds__(256) k_layer_sums_f64(const double* __restrict
         const int y = (int)(it / g.NZ), z = (int)(it - (long long)y * g.NZ);
         const double a = v.f[v.off(x, y, z)];
         cs += a;
-        if (has_flux) {
+        if (op.kind == TF_KIND_ELECTRODE) {
+            // ElectrodeSolver's plane fluxes (taufactor/electrode.py:70-74) in float64: plane 0
+            // (left_bc - c) / 0.5, plane x > 0 c[x-1] - c[x]; 0 where either value is 0
+            const double am = x > 0 ? v.f[v.off(x - 1, y, z)] : (double)op.ghost_lo;
+            double f = x > 0 ? am - a : (0.5 * (double)op.ghost_lo - a) / 0.5;
+            if (a == 0.0 || am == 0.0) f = 0.0;
+            fs += f;
+        } else if (has_flux) {
             const double d = v.f[v.off(x + 1, y, z)] - a;
             const int ca = v.code[v.offc(x, y, z)], cb = v.code[v.offc(x + 1, y, z)];
             if (op.kind == TF_KIND_MULTIPHASE) fs += (double)lut[ca * 32 + cb] * d;
@@ -198,7 +217,8 @@ __global__ void __launch_bounds__(256) k_layer_sums_f64(const double* __restrict
     }
     block_sum2(fs, cs);
     if (threadIdx.x == 0) {
-        if (has_flux) flux[(long long)b * (g.NX - 1) + x] = fs;
+        if (op.kind == TF_KIND_ELECTRODE) flux[(long long)b * g.NX + x] = fs;  // one flux per plane
+        else if (has_flux) flux[(long long)b * (g.NX - 1) + x] = fs;
         csum[(long long)b * g.NX + x] = cs;
     }
 }

@@ -1028,16 +1028,32 @@ class ElectrodeSolver(SORSolver):
         for b, v in enumerate(k):
             self._op.divisor[b] = float(v)
 
-    def refine(self, *args, **kwargs):
-        raise NotImplementedError("FP64 refinement is built for the through-transport solvers only")
+    def refine(self, tol: float = 1e-10, max_outer: int = 12, inner_half_sweeps: int | None = None,
+               omega: float | None = None):
+        """FP64 defect correction (SORSolver.refine) of the electrode operator: A c = d c - S(c)
+        with d = nn + nr k_0 in the sweep's float32 and the inlet ghost term as b. Its integer
+        part keeps clusters cut off from the inlet and from the reactive phase exactly singular, as
+        for the binary kind, so the correction uses the solver's own codes. No reference counterpart
+        (the reference iterates in float32 only). Afterwards k_x, tau_x and tau come from the
+        float64 field."""
+        self.c_x = 0
+        return super().refine(tol=tol, max_outer=max_outer, inner_half_sweeps=inner_half_sweeps, omega=omega)
+
+    def _anchored_code(self) -> torch.Tensor:
+        return self._code
 
     def _layer_sums_electrode(self):
         with torch.cuda.device(self.device):
             if self._flux_dev.shape[1] != self.Nx:
                 self._flux_dev = torch.empty((self.batch_size, self.Nx), dtype=torch.float64, device=self.device)
-            check(self._lib.tf_layer_sums(C.byref(self._geom), C.byref(self._op), _ptr(self._cur), _ptr(self._code),
-                                          _ptr(self._flux_dev), _ptr(self._csum_dev), self._stream()),
-                  "tf_layer_sums")
+            if self._field64 is not None:
+                check(self._lib.tf_layer_sums_f64(C.byref(self._geom), C.byref(self._op), _ptr(self._field64),
+                                                  _ptr(self._code), _ptr(self._flux_dev), _ptr(self._csum_dev),
+                                                  self._stream()), "tf_layer_sums_f64")
+            else:
+                check(self._lib.tf_layer_sums(C.byref(self._geom), C.byref(self._op), _ptr(self._cur),
+                                              _ptr(self._code), _ptr(self._flux_dev), _ptr(self._csum_dev),
+                                              self._stream()), "tf_layer_sums")
             flux = self._flux_dev.cpu().numpy()
             csum = self._csum_dev.cpu().numpy()
             err = int(self._err.item())

@@ -160,3 +160,25 @@ def test_refinement_with_its_own_omega_reaches_the_same_solution():
     hb = b.refine(tol=1e-12, max_outer=30, omega=2 - 3 / img.shape[0])
     assert ha[-1] < 1e-12 and hb[-1] < 1e-12
     np.testing.assert_allclose(b.D_eff, a.D_eff, rtol=1e-11, atol=0)
+
+
+@pytest.mark.parametrize("kind", ["electrode", "periodic_electrode"])
+def test_electrode_refinement_matches_fp64_oracle(kind):
+    """ElectrodeSolver's FP64 defect correction (divisor nn + nr k_0, inlet Dirichlet term,
+    closed outlet) reaches a relative residual of 1e-12, and its tau and k_x equal those of the
+    FP64 oracle's solution of the same operator (oracle/fp64.py electrode_fp64, float64 layer
+    means) to 1e-8."""
+    from oracle.fp64 import electrode_fp64
+
+    img = (np.random.default_rng(5).random((2, 20, 12, 14)) < 0.6).astype(np.uint8)
+    cls = tg.PeriodicElectrodeSolver if kind == "periodic_electrode" else tg.ElectrodeSolver
+    s = cls(img)
+    o = OracleSolve(img, kind=kind)
+    s.set_k_0(o.k_0)  # the same float32 reaction prefactors on both sides
+    s.solve(verbose=False, conv_crit=1e-3)
+    hist = s.refine(tol=1e-12, max_outer=60)
+    assert hist[-1] < 1e-12
+    o.field = s.field.cpu().numpy()  # the float32 solution; the oracle replaces its anchored part
+    tau64, kx64 = electrode_fp64(o)
+    np.testing.assert_allclose(s.tau, tau64, rtol=1e-8)
+    np.testing.assert_allclose(s.k_x, kx64, rtol=1e-7, atol=1e-10)
