@@ -27,6 +27,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import threading
 from timeit import default_timer as timer
 
 import numpy as np
@@ -39,6 +40,7 @@ from .percolation import spans_x
 from .solvers import layer_metrics, unique_labels
 
 INTERVAL = 100  # half-sweeps between convergence checks (taufactor.py:184-185)
+_CAPTURE_LOCK = threading.Lock()
 CHUNK = 32  # planes per work item of the batched sweep
 MIN_CHUNK = 8  # shortest x-chunk when few volumes remain (each chunk streams 2 K extra planes)
 RECOMPACT = 0.75  # rebuild the work list (and re-capture the graph) below this share of items
@@ -276,13 +278,17 @@ class BatchSolve:
         assert p == 0
 
     def _capture(self, conv_crit: float):
+        # one capture at a time in the process, checked against this thread's calls only, so the
+        # batches of a MultiDeviceBatchSolve (one host thread each) may capture and read back
+        # their status flags concurrently
         g = torch.cuda.CUDAGraph()
-        side = torch.cuda.Stream(self.device)
-        side.wait_stream(torch.cuda.current_stream(self.device))
-        with torch.cuda.stream(side):
-            with torch.cuda.graph(g, stream=side):
-                self._pair(conv_crit)
-        torch.cuda.current_stream(self.device).wait_stream(side)
+        with _CAPTURE_LOCK:
+            side = torch.cuda.Stream(self.device)
+            side.wait_stream(torch.cuda.current_stream(self.device))
+            with torch.cuda.stream(side):
+                with torch.cuda.graph(g, stream=side, capture_error_mode="thread_local"):
+                    self._pair(conv_crit)
+            torch.cuda.current_stream(self.device).wait_stream(side)
         return g
 
     def _resolve_paused(self, status: np.ndarray, it: int):
@@ -491,8 +497,9 @@ def split_volumes(sizes, n_parts: int):
 
 class MultiDeviceBatchSolve:
     """BatchSolve over several GPUs of one process: whole volumes per device (split_volumes),
-    one BatchSolve per device, driven from one host thread each; results come back in the
-    caller's order. No data crosses devices (each volume lives on one GPU)."""
+    one BatchSolve per entry of `devices`, one host thread per distinct device (the parts of a
+    device listed twice run in turn); results come back in the caller's order. No data crosses
+    devices (each volume lives on one GPU)."""
 
     def __init__(self, volumes, devices, periodic=False, omega=None):
         vols = [np.asarray(v) for v in volumes]
@@ -502,23 +509,27 @@ class MultiDeviceBatchSolve:
         if len(per) != n or len(om) != n:
             raise ValueError("periodic / omega must give one entry per volume")
         self.devices = [torch.device(d) for d in devices]
-        self.parts = [p for p in split_volumes([v.size for v in vols], len(self.devices))]
+        self.parts = split_volumes([v.size for v in vols], len(self.devices))
         self.batches = [BatchSolve([vols[i] for i in p], periodic=[per[i] for i in p], omega=[om[i] for i in p],
                                    device=d) if p else None for p, d in zip(self.parts, self.devices)]
         self.n = n
 
     def solve(self, **kwargs):
-        import threading
-
         errors = []
+        by_device = {}
+        for b in self.batches:
+            if b is not None:
+                by_device.setdefault(str(b.device), []).append(b)
 
-        def run(b):
+        def run(batches):
             try:
-                b.solve(**kwargs)
+                for b in batches:
+                    with torch.cuda.device(b.device):
+                        b.solve(**kwargs)
             except BaseException as e:  # re-raised on the calling thread
                 errors.append(e)
 
-        threads = [threading.Thread(target=run, args=(b,)) for b in self.batches if b is not None]
+        threads = [threading.Thread(target=run, args=(bs,)) for bs in by_device.values()]
         start = timer()
         for t in threads:
             t.start()
