@@ -470,11 +470,20 @@ def secondary_metrics(dev):
     """The metric's other parts, on the same GPU after the main measurement: converged solves/s of
     the 64-volume uneven batch against the per-volume loop (FP32, and FP32 + FP64 correction to a
     relative residual of 1e-4), and the adjoint/forward time with a central-difference check of
-    the gradient on 8 voxels of the 320^3 per-voxel conductivity field."""
+    the gradient on 8 voxels of the 320^3 per-voxel conductivity field; and the design loop cut
+    to 384^3 and 3 steps (per-step time, gradient checks)."""
     u = uneven_batch(dev, repeat=1, refine_tols=(1e-4,), reference_tol=1e-10)
     r4 = u["refined"]["0.0001"]
     a = adjoint_cost(dev, side=320, fd_voxels=8, phases=False)
+    dl = design_loop(dev, side=384, steps=3)
     return {
+        "design_loop_384_3steps": {"workload": dl["workload"] + " (the 768^3 loop cut to 384^3 and 3 steps)",
+                                   "mean_step_s": dl["mean_step_s"], "first_step_s": dl["first"]["forward_s"] +
+                                   dl["first"]["adjoint_s"], "last_step_s": dl["last"]["forward_s"] +
+                                   dl["last"]["adjoint_s"], "max_euler_rel_err": dl["max_euler_rel_err"],
+                                   "direction_fd_rel_err": dl["direction_fd_rel_err"],
+                                   "last_fp64_residual": dl["last"]["fp64_residual"],
+                                   "last_adjoint_residual": dl["last"]["adjoint_residual"]},
         "uneven_batch": {"workload": u["workload"], "batched_solves_per_s": u["batched_solves_per_s"],
                          "per_volume_loop_solves_per_s": u["per_volume_loop_solves_per_s"],
                          "speedup_vs_loop": u["speedup"], "refined_1e-4_solves_per_s": r4["solves_per_s"],
@@ -740,13 +749,27 @@ def impedance_throughput(dev, side=256, nyq_side=64, cpu_half_sweeps=4):
     r = b.solve_frequencies()
     torch.cuda.synchronize()
     t_bat = time.perf_counter() - t3
-    # frequencies that both runs converged with a finite, non-zero impedance (a NaN field ends a
-    # frequency with its impedance left at 0; in Nyquist mode the sequential run keeps no tau)
-    imp_a = np.array([complex(z) for z in a.impedance])
+    # Red-black SOR with the reference's omega is unstable on this complex operator at the high
+    # end of the sweep: fields grow to ~1e278 while the relative-error test still passes, so an
+    # "impedance" of ~1e-278 is returned, and the sequential loop carries that field into every
+    # lower frequency (it re-initialises only after a NaN). Physically meaningful results: the
+    # converged, finite impedances of sane magnitude. The sequential loop is therefore run again
+    # from the first frequency that solve_frequencies solved sanely, and the two are compared there.
     imp_b = np.asarray(r["impedance"])
-    both = (np.array(a.converged_freq, dtype=bool) & np.asarray(r["converged"], dtype=bool)
-            & np.isfinite(imp_a) & (imp_a != 0) & np.isfinite(imp_b) & (imp_b != 0))
-    agree = [abs(complex(a.impedance[k]) - r["impedance"][k]) / abs(r["impedance"][k]) for k in np.flatnonzero(both)]
+    sane_b = np.asarray(r["converged"], dtype=bool) & np.isfinite(imp_b) & (np.abs(imp_b) > 1e-12) & \
+        (np.abs(imp_b) < 1e12)
+    agree, k0, a2 = [], None, None
+    if sane_b.any():
+        k0 = int(np.flatnonzero(sane_b)[0])
+        with contextlib.redirect_stdout(io.StringIO()):
+            a2 = tg.ImpedanceSolver(nv, device=dev, mode="nyquist")
+            a2.frequency = a2.frequency[k0:]
+            a2.solve(verbose=False)
+        imp_a = np.array([complex(z) for z in a2.impedance])
+        sane_a = np.array(a2.converged_freq, dtype=bool) & np.isfinite(imp_a) & (np.abs(imp_a) > 1e-12) & \
+            (np.abs(imp_a) < 1e12)
+        both = sane_a & sane_b[k0:]
+        agree = [abs(imp_a[k] - imp_b[k0 + k]) / abs(imp_b[k0 + k]) for k in np.flatnonzero(both)]
     return {"workload": f"ImpedanceSolver {side}^3 pore volume (porosity 0.45, sigma 2, rng 5000; isolated pores inert)",
             "dtype": "complex128", "half_sweeps": int(s.sum_iter), "converged_freq": s.converged_freq,
             "taus": [float(np.asarray(v)[0]) for v in s.taus], "solve_s": t, "voxel_updates_per_s": vu / t,
@@ -759,8 +782,13 @@ def impedance_throughput(dev, side=256, nyq_side=64, cpu_half_sweeps=4):
                         "sequential_converged": int(sum(a.converged_freq)),
                         "side_by_side_s": t_bat, "side_by_side_half_sweeps": [int(v) for v in r["iters"]],
                         "side_by_side_converged": int(r["converged"].sum()),
-                        "both_converged_finite": int(both.sum()),
-                        "max_rel_diff_converged": float(max(agree)) if agree else None}}
+                        "side_by_side_sane": int(sane_b.sum()),
+                        "blown_up_frequencies": int(np.sum(np.isfinite(imp_b) & (np.abs(imp_b) <= 1e-12))),
+                        "sequential_from_first_sane": k0,
+                        "compared_frequencies": len(agree),
+                        "max_rel_diff_converged": float(max(agree)) if agree else None,
+                        "note": "the sequential loop warm-starts each frequency from the previous one; "
+                                "both stop at the reference's conv_crit 1e-3"}}
 
 
 def adjoint_cost(dev, side=320, fd_voxels=0, tol=1e-12, fd_tol=1e-14, phases=True):
