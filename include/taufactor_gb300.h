@@ -385,6 +385,49 @@ int tf_kappa_gradient(const tf_geom* g, const tf_operator* op, const double* fie
 /* double field layout -> natural [batch][nx][ny][nz]. */
 int tf_split_to_natural_f64(const tf_geom* g, const double* split_dev, double* natural_dev, void* stream);
 
+/* ---- Multigrid-preconditioned conjugate gradients for the correction solve A e = r ---------
+ * No reference counterpart: the reference solves only by red-black SOR (taufactor.py:156-191).
+ * These serve the float32 inner solve of the FP64 defect correction (KappaSolver). A level is a
+ * tf_geom of dims (nx, ny, nz), the next one of dims ((nx+1)/2, (ny+1)/2, (nz+1)/2) and the same
+ * batch, each with packed faces in the tf_kappa_faces layout; its smoother is
+ * tf_kappa_advance_faces with omega 1 and ghost values 0. Dirichlet x ghosts are 0 throughout. */
+
+/* Coarse faces and factor: `scale` times the sum of the fine faces across each coarse interface
+ * (aggregates of 2 cells per axis, 1 at the end of an odd extent), the factor their sum in the
+ * order of tf_kappa_faces with the Dirichlet x faces counted twice; periodic ghost positions hold
+ * the wrapped cell's faces (TF_PERIODIC_* bits of `periodic`), closed ones 0 (factor inf). */
+int tf_mg_coarsen(const tf_geom* fine, const float* fx_dev, const float* fy_dev, const float* fz_dev,
+                  const tf_geom* coarse, float* cfx_dev, float* cfy_dev, float* cfz_dev, float* cdiv_dev,
+                  int periodic, float scale, void* stream);
+
+/* Coarse right-hand side rc = sum over each aggregate of (rhs - A e) on the fine level (rhs_dev
+ * may be NULL); writes the coarse interior cells only. */
+int tf_mg_restrict(const tf_geom* fine, const float* e_dev, const float* rhs_dev, const float* fx_dev,
+                   const float* fy_dev, const float* fz_dev, const float* div_dev, const tf_geom* coarse,
+                   float* rc_dev, void* stream);
+
+/* e += the coarse value of its aggregate on every fine interior cell; periodic ghosts rebuilt. */
+int tf_mg_prolong(const tf_geom* coarse, const float* ec_dev, const tf_geom* fine, float* e_dev, int periodic,
+                  void* stream);
+
+/* out = A in on interior cells (0 where the factor is not finite); other cells untouched. The
+ * ghost cells of in_dev must be current (periodic copies or 0). */
+int tf_mg_apply(const tf_geom* g, const float* in_dev, const float* fx_dev, const float* fy_dev,
+                const float* fz_dev, const float* div_dev, float* out_dev, void* stream);
+
+/* Per-volume float64 dot products over interior cells, in a fixed order: out[b] = sum a1*b1 and,
+ * when a2_dev/b2_dev are given, out[batch + b] = sum a2*b2. part_dev: double [2 * batch*nx*ny]. */
+int tf_mg_dot(const tf_geom* g, const float* a1_dev, const float* b1_dev, const float* a2_dev, const float* b2_dev,
+              double* part_dev, double* out_dev, void* stream);
+
+/* Conjugate-gradient updates over whole volumes with per-volume steps (0 where a denominator is
+ * not a positive finite number): x += a p, r -= a q with a = rz[b] / pq[b]; p = z + c p with
+ * c = rz_new[b] / rz_old[b]. Pointers 16-byte aligned. */
+int tf_pcg_update_xr(const tf_geom* g, float* x_dev, float* r_dev, const float* p_dev, const float* q_dev,
+                     const double* rz_dev, const double* pq_dev, void* stream);
+int tf_pcg_update_p(const tf_geom* g, float* p_dev, const float* z_dev, const double* rz_new_dev,
+                    const double* rz_old_dev, void* stream);
+
 /* ---- Impedance (tau_e) solve: ImpedanceSolver / PeriodicImpedanceSolver ----------------------
  * (taufactor/electrode.py:160-402). One volume; n_freq frequencies solved side by side. The field
  * is complex128 in the reference's padded layout [n_freq][nx+2][ny+2][nz+2], interleaved

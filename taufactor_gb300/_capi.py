@@ -29,7 +29,8 @@ EXPORTS = (
     "tf_kappa_faces", "tf_kappa_advance_faces", "tf_spans_x",
     "tf_impedance_pack", "tf_impedance_fill", "tf_impedance_sweep", "tf_impedance_metrics",
     "tf_batch_advance_tile", "tf_batch_advance_rhs_tile", "tf_label_stats", "tf_anchored_phase",
-    "tf_kappa_stats",
+    "tf_kappa_stats", "tf_mg_coarsen", "tf_mg_restrict", "tf_mg_prolong", "tf_mg_apply", "tf_mg_dot",
+    "tf_pcg_update_xr", "tf_pcg_update_p",
 )
 TF_IMP_TABLE = 56
 TF_BATCH_ACTIVE, TF_BATCH_CONVERGED, TF_BATCH_NEEDS_HOST = 0, 1, 2
@@ -128,6 +129,13 @@ def load():
         "tf_kappa_adjoint_rhs": (i32, [G, vp, vp, C.c_double, i32, vp]),
         "tf_kappa_gradient": (i32, [G, O, vp, vp, vp, vp, C.c_double, C.c_double, C.c_double, vp]),
         "tf_split_to_natural_f64": (i32, [G, vp, vp, vp]),
+        "tf_mg_coarsen": (i32, [G, vp, vp, vp, G, vp, vp, vp, vp, i32, C.c_float, vp]),
+        "tf_mg_restrict": (i32, [G, vp, vp, vp, vp, vp, vp, G, vp, vp]),
+        "tf_mg_prolong": (i32, [G, vp, G, vp, i32, vp]),
+        "tf_mg_apply": (i32, [G, vp, vp, vp, vp, vp, vp, vp]),
+        "tf_mg_dot": (i32, [G, vp, vp, vp, vp, vp, vp, vp]),
+        "tf_pcg_update_xr": (i32, [G, vp, vp, vp, vp, vp, vp, vp]),
+        "tf_pcg_update_p": (i32, [G, vp, vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

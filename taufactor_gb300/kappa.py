@@ -18,6 +18,13 @@ faces (``coefficients="f32"``, the reference's operator and what the float32 swe
 moves in steps of one float32 rounding of a face, which puts about 1e-7/h relative noise into a
 central difference of step h. The two refined D_eff differ by about 1e-7 relative.
 
+The inner solve of each FP64 correction step is either the float32 SOR sweeps
+(``inner="sor"``) or conjugate gradients preconditioned by a multigrid V-cycle
+(``inner="mg"``, ``multigrid.KappaMultigrid``); ``"auto"`` (the default) takes multigrid when
+kappa > 0 everywhere, where every cluster touches the Dirichlet faces, and SOR otherwise.
+``solve(method="mg")`` skips the float32 SOR loop and runs the FP64 correction with multigrid
+inner solves from the current field (the initial profile or a warm start).
+
 The reference runs its solve under ``torch.no_grad()`` (taufactor.py:172); gradients are pinned
 by central finite differences and by an FP64 adjoint on the CPU (``oracle/fp64.py``).
 """
@@ -84,6 +91,9 @@ class KappaSolver:
             pos_h, sums_h, bad_h = pos.cpu().numpy(), sums.cpu().numpy(), int(bad.item())
         if bad_h:
             raise ValueError("kappa must be finite and >= 0")
+        # every voxel conductive: every cluster touches both x faces, A is nonsingular
+        self.all_positive = int(pos_h.sum()) == B * X * Y * Z
+        self._mg = None
         self.vol_x = pos_h / float(Y * Z)
         self.D_mean = sums_h.sum(axis=1) / float(X * Y * Z)
         self.cpu_img = None  # built lazily for the percolation fallback
@@ -149,9 +159,21 @@ class KappaSolver:
         self.flux_1d, c_x = self._layer_means()
         return layer_metrics(self, self.flux_1d, c_x)
 
-    def solve(self, iter_limit=10000, conv_crit=1e-2, verbose=False, refine=False):
-        """The reference's loop and convergence rule (taufactor.py:156-191) on this operator."""
+    def solve(self, iter_limit=10000, conv_crit=1e-2, verbose=False, refine=False, method="sor"):
+        """The reference's loop and convergence rule (taufactor.py:156-191) on this operator
+        (method "sor"), then `refine` (False, True or refine()'s keyword arguments). method "mg":
+        no float32 loop; the FP64 correction with multigrid inner solves from the current field
+        (refine's tol, default 1e-11), converged when its residual reaches tol."""
+        if method not in ("sor", "mg"):
+            raise ValueError('method must be "sor" or "mg"')
         start = timer()
+        if method == "mg":
+            opts = dict(refine) if isinstance(refine, dict) else {}
+            opts.setdefault("inner", "mg")
+            hist = self.refine(**opts)
+            self.converged = bool(hist[-1] < opts.get("tol", 1e-11))
+            self.walltime = timer() - start
+            return self.tau_x
         with torch.cuda.device(self.device):
             while not self.converged and self.iter < iter_limit:
                 n = min(100 - self.iter % 100, iter_limit - self.iter)
@@ -187,8 +209,25 @@ class KappaSolver:
         self.converged = False
         self.old_tau = 0
 
-    def _fp64_solve(self, x64, b64, tol, max_outer, n_inner):
-        """FP64 defect correction for A x = b (b64 None: the Dirichlet terms); returns history."""
+    def _inner(self, inner: str) -> str:
+        if inner not in ("auto", "sor", "mg"):
+            raise ValueError('inner must be "auto", "sor" or "mg"')
+        if inner == "auto":
+            return "mg" if self.all_positive else "sor"
+        return inner
+
+    def multigrid(self):
+        """The multigrid preconditioner of the inner solves (built on first use)."""
+        if self._mg is None:
+            from .multigrid import KappaMultigrid
+
+            self._mg = KappaMultigrid(self)
+        return self._mg
+
+    def _fp64_solve(self, x64, b64, tol, max_outer, n_inner, inner="sor", inner_rtol=1e-5):
+        """FP64 defect correction for A x = b (b64 None: the Dirichlet terms); returns history.
+        Inner solve of A e = r: n_inner float32 SOR half-sweeps from e = 0, or multigrid
+        conjugate gradients to a relative residual of inner_rtol."""
         g, lib, st = self._geom, self._lib, self._stream()
         op0 = TfOperator.from_buffer_copy(self._op)
         op0.ghost_lo = op0.ghost_hi = 0.0
@@ -205,20 +244,26 @@ class KappaSolver:
             hist.append(rel)
             if rel < tol or outer == max_outer:
                 break
-            e.zero_()
-            self._advance(n_inner, e, rhs=rhs, op=op0, first_colour=0)
+            if inner == "mg":
+                self.multigrid().solve(e, rhs, rtol=inner_rtol, max_iter=max(50, n_inner // 4))
+            else:
+                e.zero_()
+                self._advance(n_inner, e, rhs=rhs, op=op0, first_colour=0)
             check(lib.tf_axpy_f64(C.byref(g), _ptr(x64), _ptr(e), st), "tf_axpy_f64")
         return hist
 
-    def refine(self, tol: float = 1e-11, max_outer: int = 12, inner_half_sweeps=None):
-        """FP64 defect correction of the converged field; metrics from the float64 field."""
+    def refine(self, tol: float = 1e-11, max_outer: int = 12, inner_half_sweeps=None, inner="auto"):
+        """FP64 defect correction of the converged field; metrics from the float64 field.
+        inner: "sor" (inner_half_sweeps float32 half-sweeps per step), "mg" (multigrid conjugate
+        gradients) or "auto" (multigrid where kappa > 0 everywhere)."""
         t0 = timer()
+        inner = self._inner(inner)
         n_inner = inner_half_sweeps or max(400, 2 * (self.iter or 200))
         with torch.cuda.device(self.device):
             g, lib, st = self._geom, self._lib, self._stream()
             c64 = torch.empty(g.field_elems, dtype=torch.float64, device=self.device)
             check(lib.tf_widen_f64(C.byref(g), _ptr(self._c), _ptr(c64), st), "tf_widen_f64")
-            self.residual_history = self._fp64_solve(c64, None, tol, max_outer, n_inner)
+            self.residual_history = self._fp64_solve(c64, None, tol, max_outer, n_inner, inner)
             check(lib.tf_narrow_f64(C.byref(g), C.byref(self._op), _ptr(c64), _ptr(self._c), st), "tf_narrow_f64")
             self._c64 = c64
             self.tau, _ = self.compute_metrics()
@@ -228,13 +273,15 @@ class KappaSolver:
         return self.residual_history
 
     # ---------------------------------------------------------------- adjoint
-    def gradient(self, tol: float = 1e-11, max_outer: int = 12, inner_half_sweeps=None, lam0=None) -> torch.Tensor:
+    def gradient(self, tol: float = 1e-11, max_outer: int = 12, inner_half_sweeps=None, lam0=None,
+                 inner="auto") -> torch.Tensor:
         """dD_eff/dkappa [B,X,Y,Z] (float64, on the device) at the current (refined) solution.
 
         lam0: optional starting adjoint field (another solver's `lam` of the same shape, e.g. the
-        previous step of a design loop); the adjoint field is kept as `lam`."""
+        previous step of a design loop); the adjoint field is kept as `lam`. inner: as refine()."""
+        inner = self._inner(inner)
         if self._c64 is None:
-            self.refine(tol=tol)
+            self.refine(tol=tol, inner=inner)
         t0 = timer()
         n_inner = inner_half_sweeps or max(400, 2 * (self.iter or 200))
         scale = self.D_0 * self.Nx / (abs(self.bot_bc - self.top_bc) * (self.Nx - 1) * self.Ny * self.Nz)
@@ -249,7 +296,7 @@ class KappaSolver:
                 lam = lam0.to(device=self.device, dtype=torch.float64).clone()
             else:
                 lam = torch.zeros(g.field_elems, dtype=torch.float64, device=self.device)
-            self.adjoint_history = self._fp64_solve(lam, dj, tol, max_outer, n_inner)
+            self.adjoint_history = self._fp64_solve(lam, dj, tol, max_outer, n_inner, inner)
             self.lam = lam
             grad = torch.empty((self.batch_size, self.Nx, self.Ny, self.Nz), dtype=torch.float64, device=self.device)
             check(lib.tf_kappa_gradient(C.byref(g), C.byref(self._op), _ptr(self._c64), _ptr(lam), _ptr(self._ks),
@@ -274,9 +321,10 @@ class DeffFunction(torch.autograd.Function):
     backward = adjoint solve. Saves only the solver with its converged field."""
 
     @staticmethod
-    def forward(ctx, kappa: torch.Tensor, periodic: bool = False, conv_crit: float = 1e-3, tol: float = 1e-11):
+    def forward(ctx, kappa: torch.Tensor, periodic: bool = False, conv_crit: float = 1e-3, tol: float = 1e-11,
+                method: str = "sor"):
         s = KappaSolver(kappa.detach(), periodic=periodic, device=kappa.device)
-        s.solve(conv_crit=conv_crit, refine={"tol": tol})
+        s.solve(conv_crit=conv_crit, refine={"tol": tol}, method=method)
         ctx.solver = s
         ctx.tol = tol
         ctx.squeeze = kappa.dim() == 3
@@ -289,9 +337,11 @@ class DeffFunction(torch.autograd.Function):
         g = s.gradient(tol=ctx.tol)
         go = grad_out.reshape(-1, 1, 1, 1).to(g.dtype)
         grad = (g * go).to(torch.float32)
-        return (grad[0] if ctx.squeeze else grad), None, None, None
+        return (grad[0] if ctx.squeeze else grad), None, None, None, None
 
 
-def d_eff(kappa: torch.Tensor, periodic: bool = False, conv_crit: float = 1e-3, tol: float = 1e-11) -> torch.Tensor:
-    """Differentiable D_eff of a per-voxel conductivity field (float64 result)."""
-    return DeffFunction.apply(kappa, periodic, conv_crit, tol)
+def d_eff(kappa: torch.Tensor, periodic: bool = False, conv_crit: float = 1e-3, tol: float = 1e-11,
+          method: str = "sor") -> torch.Tensor:
+    """Differentiable D_eff of a per-voxel conductivity field (float64 result); method as
+    KappaSolver.solve."""
+    return DeffFunction.apply(kappa, periodic, conv_crit, tol, method)
