@@ -478,7 +478,7 @@ def secondary_metrics(dev):
     dl = design_loop(dev, side=384, steps=3)
     return {
         "design_loop_384_3steps": {"workload": dl["workload"] + " (the 768^3 loop cut to 384^3 and 3 steps)",
-                                   "mean_step_s": dl["mean_step_s"], "first_step_s": dl["first"]["forward_s"] +
+                                   "method": dl["method"], "mean_step_s": dl["mean_step_s"], "first_step_s": dl["first"]["forward_s"] +
                                    dl["first"]["adjoint_s"], "last_step_s": dl["last"]["forward_s"] +
                                    dl["last"]["adjoint_s"], "max_euler_rel_err": dl["max_euler_rel_err"],
                                    "direction_fd_rel_err": dl["direction_fd_rel_err"],
@@ -491,8 +491,11 @@ def secondary_metrics(dev):
                          "max_rel_D_eff_vs_fp64": u["max_rel_D_eff_loop_vs_fp64"],
                          "refined_1e-4_max_rel_D_eff_vs_fp64": r4["max_rel_D_eff_vs_fp64"],
                          "max_rel_D_eff_batched_vs_loop": u["max_rel_D_eff_batched_vs_loop"]},
-        "adjoint": {"workload": a["workload"], "forward_s": a["forward_s"], "adjoint_s": a["adjoint_s"],
-                    "adjoint_over_forward": a["adjoint_over_forward"], "fd_voxels": a["fd_voxels"],
+        "adjoint": {"workload": a["workload"], "inner_solve": a["inner_solve"], "forward_s": a["forward_s"],
+                    "adjoint_s": a["adjoint_s"], "adjoint_over_forward": a["adjoint_over_forward"],
+                    "forward_multigrid_only_s": a["forward_multigrid_only_s"],
+                    "sor_inner_forward_s": a["sor_inner"]["forward_s"], "sor_inner_adjoint_s": a["sor_inner"]["adjoint_s"],
+                    "fd_voxels": a["fd_voxels"],
                     "fd_h": a["fd_h"], "fd_max_rel_err": a["fd_max_rel_err"],
                     "fd_direction_rel_err": a["fd_direction_rel_err"], "euler_rel_err": a["euler_rel_err"]},
     }
@@ -566,14 +569,17 @@ def uneven_batch(dev, conv_crit=CONV_CRIT, repeat=2, refine_tols=(1e-4, 1e-6, 1e
             "timing": "wall clock excl. input generation and solver construction"}
 
 
-def design_loop(dev, side=768, steps=50, lr=0.05, lam=0.5, tol=1e-8, conv_crit=1e-3):
+def design_loop(dev, side=768, steps=50, lr=0.05, lam=0.5, tol=1e-8, conv_crit=1e-3, method="mg"):
     """Gradient-driven design loop on one side^3 volume: kappa = sigmoid(logits), logits =
     blur_sigma4(N(0,1)) from default_rng(5000); Adam on the logits maximising
     D_eff - lam * mean(kappa). Every step: forward solve warm-started from the previous step's
-    field, FP64 refinement to a relative residual of tol, adjoint solve warm-started from the
-    previous adjoint field. Reports per-step times, the solve and adjoint residuals, Euler's
+    field to an FP64 relative residual of tol, adjoint solve warm-started from the previous
+    adjoint field. method "mg": FP64 correction with multigrid conjugate-gradient inner solves
+    from the warm start (no float32 loop), adjoint likewise; "sor": the float32 loop to conv_crit
+    and SOR inner solves. Reports per-step times, the solve and adjoint residuals, Euler's
     identity sum(kappa dD/dkappa) = D_eff per step and, at the last step, a directional central
     difference along the update direction."""
+    inner = "mg" if method == "mg" else "sor"
     import torch
     from scipy.ndimage import gaussian_filter
 
@@ -593,10 +599,10 @@ def design_loop(dev, side=768, steps=50, lr=0.05, lam=0.5, tol=1e-8, conv_crit=1
         s = tg.KappaSolver(kap, device=dev)
         if prev is not None:
             s.warm_start(prev)
-        s.solve(conv_crit=conv_crit, refine={"tol": tol, "max_outer": 40})
+        s.solve(conv_crit=conv_crit, refine={"tol": tol, "max_outer": 40, "inner": inner}, method=method)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
-        g = s.gradient(tol=tol, max_outer=40, lam0=prev.lam if prev is not None else None)[0]
+        g = s.gradient(tol=tol, max_outer=40, lam0=prev.lam if prev is not None else None, inner=inner)[0]
         torch.cuda.synchronize()
         t2 = time.perf_counter()
         d = float(s.D_eff[0])
@@ -622,7 +628,7 @@ def design_loop(dev, side=768, steps=50, lr=0.05, lam=0.5, tol=1e-8, conv_crit=1
         def deff(kk):
             t = tg.KappaSolver(kk.contiguous(), device=dev)
             t.warm_start(prev)
-            t.solve(conv_crit=conv_crit, refine={"tol": 1e-13, "max_outer": 40})
+            t.solve(conv_crit=conv_crit, refine={"tol": 1e-13, "max_outer": 40, "inner": inner}, method=method)
             return float(t.D_eff[0])
 
         kp = (kap + h * direc).float()
@@ -631,7 +637,7 @@ def design_loop(dev, side=768, steps=50, lr=0.05, lam=0.5, tol=1e-8, conv_crit=1
         step = ((kp.double() - km.double()) / 2.0)
         ad = float((g * step).sum())
     return {"workload": f"design loop {side}^3, kappa = sigmoid(logits), logits = blur_sigma4(N(0,1)) rng 5000, "
-                        f"Adam lr {lr} on D_eff - {lam} mean(kappa)", "steps": steps, "total_s": total,
+                        f"Adam lr {lr} on D_eff - {lam} mean(kappa)", "method": method, "steps": steps, "total_s": total,
             "mean_step_s": total / steps, "first": rows[0], "last": rows[-1],
             "max_euler_rel_err": max(r["euler_rel_err"] for r in rows),
             "direction_fd_rel_err": abs(fd - ad) / abs(fd), "fd_h": h, "per_step": rows}
@@ -805,22 +811,36 @@ def adjoint_cost(dev, side=320, fd_voxels=0, tol=1e-12, fd_tol=1e-14, phases=Tru
     warm.gradient(tol=tol)
     logits = gaussian_filter(2.0 * np.random.default_rng(3003).standard_normal((side,) * 3, dtype=np.float32), 2.0)
     kap = (1.0 / (1.0 + np.exp(-logits))).astype(np.float32)
-    s = tg.KappaSolver(kap, device=dev)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    s.solve(conv_crit=1e-3, refine={"tol": tol})
-    torch.cuda.synchronize()
-    t_fwd = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    g = s.gradient(tol=tol)
-    torch.cuda.synchronize()
-    t_adj = time.perf_counter() - t0
-    out = {"workload": f"kappa field {side}^3 = sigmoid(blur_sigma2(2 N(0,1)))", "forward_s": t_fwd,
-           "adjoint_s": t_adj, "adjoint_over_forward": t_adj / t_fwd, "half_sweeps_forward": s.iter,
+    def timed(inner, method="sor"):
+        s = tg.KappaSolver(kap, device=dev)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.solve(conv_crit=1e-3, refine={"tol": tol, "inner": inner}, method=method)
+        torch.cuda.synchronize()
+        t_fwd = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        g = s.gradient(tol=tol, inner=inner)
+        torch.cuda.synchronize()
+        return s, g, t_fwd, time.perf_counter() - t0
+
+    # the default: the reference's float32 loop to conv_crit, then FP64 correction and adjoint
+    # with multigrid conjugate-gradient inner solves
+    s, g, t_fwd, t_adj = timed("mg")
+    s_sor, _, f_sor, a_sor = timed("sor")
+    s_mg, _, f_mg, _ = timed("mg", method="mg")
+    out = {"workload": f"kappa field {side}^3 = sigmoid(blur_sigma2(2 N(0,1)))", "inner_solve": "multigrid PCG",
+           "forward_s": t_fwd, "adjoint_s": t_adj, "adjoint_over_forward": t_adj / t_fwd,
+           "half_sweeps_forward": s.iter, "pcg_iterations": [int(i) for i, _ in s.multigrid().history],
            "fp64_residual": s.residual_history[-1], "adjoint_residual": s.adjoint_history[-1],
            "D_eff": float(s.D_eff[0]),
            # D_eff is homogeneous of degree 1 in kappa, so sum(kappa * dD_eff/dkappa) = D_eff
-           "euler_rel_err": abs(float((s.kappa.double() * g).sum()) - float(s.D_eff[0])) / float(s.D_eff[0])}
+           "euler_rel_err": abs(float((s.kappa.double() * g).sum()) - float(s.D_eff[0])) / float(s.D_eff[0]),
+           "forward_multigrid_only_s": f_mg, "forward_multigrid_only_D_eff_rel_diff":
+               abs(float(s_mg.D_eff[0]) / float(s.D_eff[0]) - 1.0),
+           "sor_inner": {"forward_s": f_sor, "adjoint_s": a_sor, "outer_steps": len(s_sor.residual_history) - 1,
+                         "adjoint_outer_steps": len(s_sor.adjoint_history) - 1,
+                         "D_eff_rel_diff": abs(float(s_sor.D_eff[0]) / float(s.D_eff[0]) - 1.0)}}
+    del s_sor, s_mg
     # per-phase gradients of MultiPhaseSolver on the three-label volume (labels = argmax of three
     # blurred fields, default_rng(3000..3002), D = {0: 0, 1: 1, 2: 0.1}) against central
     # differences in D_1 and D_2 of the operator they differentiate: kappa = D[label] with float64
@@ -968,6 +988,8 @@ def main():
     ap.add_argument("--adj-side", dest="adj_side", type=int, default=320, help="--workload adjoint: volume side")
     ap.add_argument("--design-side", type=int, default=768, help="--workload design: volume side")
     ap.add_argument("--design-steps", type=int, default=50, help="--workload design: Adam steps")
+    ap.add_argument("--design-method", choices=["mg", "sor"], default="mg",
+                    help="--workload design: multigrid inner solves (mg) or the float32 loop + SOR (sor)")
     args = ap.parse_args()
     if args.workload:
         import torch
@@ -980,7 +1002,8 @@ def main():
         elif args.workload == "impedance":
             print(json.dumps(impedance_throughput(dev)), flush=True)
         elif args.workload == "design":
-            print(json.dumps(design_loop(dev, args.design_side, args.design_steps)), flush=True)
+            print(json.dumps(design_loop(dev, args.design_side, args.design_steps, method=args.design_method)),
+                  flush=True)
         else:
             print(json.dumps(adjoint_cost(dev, args.adj_side, args.fd_voxels)), flush=True)
     elif args.profile:
