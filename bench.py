@@ -949,6 +949,19 @@ def run_profile(args):
         torch.cuda.synchronize()
         print(f"profile workload done: impedance {args.side}^3, {args.half_sweeps} half-sweeps")
         return
+    if args.multigrid:  # KappaSolver --side^3 (C4 generator, rng 3003): one FP64 correction, multigrid PCG
+        from scipy.ndimage import gaussian_filter
+
+        lg = gaussian_filter(2.0 * np.random.default_rng(3003).standard_normal((args.side,) * 3, dtype=np.float32), 2.0)
+        kap = (1.0 / (1.0 + np.exp(-lg))).astype(np.float32)
+        s = tg.KappaSolver(kap, device="cuda")
+        s.multigrid()
+        torch.cuda.synchronize()
+        s.solve(method="mg", refine={"tol": 1e-8})
+        torch.cuda.synchronize()
+        print(f"profile workload done: multigrid correction {args.side}^3, PCG iterations "
+              f"{[i for i, _ in s.multigrid().history]}")
+        return
     vols = batch_256(args.batch, args.side, SIGMA)
     cls = tg.PeriodicSolver if args.periodic else tg.Solver
     s = cls(vols, device="cuda")
@@ -980,6 +993,8 @@ def main():
     ap.add_argument("--side", type=int, default=256, help="--profile: volume side")
     ap.add_argument("--half-sweeps", type=int, default=40, help="--profile: half-sweeps")
     ap.add_argument("--periodic", action="store_true", help="--profile: PeriodicSolver")
+    ap.add_argument("--multigrid", action="store_true",
+                    help="--profile: one multigrid-PCG FP64 correction of a --side^3 kappa field")
     ap.add_argument("--impedance", action="store_true", help="--profile: ImpedanceSolver on one volume")
     ap.add_argument("--uneven", action="store_true", help="--profile: one batched solve of the uneven batch")
     ap.add_argument("--workload", choices=["uneven", "adjoint", "design", "electrode", "impedance"], default=None,

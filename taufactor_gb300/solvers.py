@@ -221,28 +221,107 @@ class SORSolver:
         return autotune.tune(self, half_sweeps)
 
     def refine(self, tol: float = 1e-10, max_outer: int = 12, inner_half_sweeps: int | None = None,
-               omega: float | None = None):
+               omega: float | None = None, inner: str = "sor"):
         """FP64 defect correction of the current field; returns the relative residual history.
 
         Keeps the solution in float64, forms r = b - A c in float64 on the device, solves A e = r
-        with the float32 sweeps (right-hand side r, homogeneous Dirichlet faces, same omega) and
-        adds e in float64, until max over volumes of ||r|| / ||b|| < tol. The reference has no
-        such step (it iterates in float32 only, taufactor.py:172-182). Afterwards the metrics
-        (D_eff, tau, flux_1d, c_x, tau_x) come from the float64 field and the float32 field holds
-        its rounding. omega: over-relaxation of the correction sweeps (default: the solve's own;
+        approximately in float32 and adds e in float64, until max over volumes of ||r|| / ||b||
+        < tol. The reference has no such step (it iterates in float32 only,
+        taufactor.py:172-182). Afterwards the metrics (D_eff, tau, flux_1d, c_x, tau_x) come from
+        the float64 field and the float32 field holds its rounding.
+
+        inner: "sor" solves A e = r by inner_half_sweeps float32 sweeps (right-hand side r,
+        homogeneous Dirichlet faces; omega: their over-relaxation, default the solve's own;
         2 - 3/Nx needed 9 instead of 13 outer steps on a 256^3 binary volume and 14 instead of 15
-        on a 320^3 three-label one).
+        on a 320^3 three-label one). "mg" (binary and multiphase kinds) solves it by conjugate
+        gradients preconditioned with a multigrid V-cycle on the same operator, written as
+        per-voxel faces (multigrid.KappaMultigrid), to a relative residual of 1e-5; clusters that
+        touch neither x face are frozen for it (the anchored system of the FP64 oracle).
         """
+        if inner not in ("sor", "mg"):
+            raise ValueError('inner must be "sor" or "mg"')
         n_inner = inner_half_sweeps or max(400, 2 * (self.iter or 200))
+        solve_e = None
         with torch.cuda.device(self.device):
-            code = self._code if self._kind == TF_KIND_BINARY else self._anchored_code()
+            if inner == "mg":
+                mg = self.multigrid()
+                code = self._anchored_code()
+
+                def solve_e(e, r):
+                    mg.solve(e, r, rtol=1e-5, max_iter=max(50, n_inner // 4))
+            else:
+                code = self._code if self._kind == TF_KIND_BINARY else self._anchored_code()
             c64, hist = refine_field(self._lib, self._geom, self._op, self._cur, code, self._err,
-                                     self._stream(), self.batch_size, tol, max_outer, n_inner, omega)
+                                     self._stream(), self.batch_size, tol, max_outer, n_inner, omega, solve_e)
         self._field64 = c64
         self.residual_history = hist
         self.tau, _ = self.compute_metrics()
         self.tau = np.where(self.tau == 0, np.inf, self.tau)
         return hist
+
+    def _phase_conductivities(self) -> np.ndarray:
+        """float32 conductivity of every phase index of the packed phase map (256 entries)."""
+        t = np.zeros(256, dtype=np.float32)
+        t[1] = 1.0
+        return t
+
+    def multigrid(self):
+        """Multigrid preconditioner of refine(inner="mg"): the operator on the anchored phase
+        map written as per-voxel faces (kappa = conductivity of the phase index; for the binary
+        kind the faces are 1 between conductive neighbours, counted twice on the Dirichlet faces,
+        so the factor is the neighbour count of the sweeps)."""
+        cached = getattr(self, "_mg", None)
+        if cached is not None:
+            return cached
+        if self._kind not in (TF_KIND_BINARY, TF_KIND_MULTIPHASE):
+            raise ValueError("multigrid inner solves need the binary or the multiphase operator")
+        from types import SimpleNamespace
+
+        from .multigrid import KappaMultigrid
+
+        g, dev, st = self._geom, self.device, self._stream()
+        phase = self._anchored_phase()
+        table = torch.from_numpy(self._phase_conductivities()).to(dev)
+        kap = table[phase.long()]
+        del phase
+        f32 = dict(dtype=torch.float32, device=dev)
+        ks = torch.empty(g.field_elems, **f32)
+        scratch = torch.empty(g.field_elems, **f32)
+        check(self._lib.tf_kappa_pack(C.byref(g), C.byref(self._op), _ptr(kap), _ptr(self._profile_dev), _ptr(ks),
+                                      _ptr(scratch), st), "tf_kappa_pack")
+        del kap, scratch
+        plane = g.field_elems // (self.batch_size * self.Nx)
+        fx = torch.empty(self.batch_size * (self.Nx + 1) * plane, **f32)
+        fy, fz, dv = (torch.empty(g.field_elems, **f32) for _ in range(3))
+        check(self._lib.tf_kappa_faces(C.byref(g), _ptr(ks), _ptr(fx), _ptr(fy), _ptr(fz), _ptr(dv), st),
+              "tf_kappa_faces")
+        del ks
+        view = SimpleNamespace(device=dev, _op=self._op, batch_size=self.batch_size, Nx=self.Nx, Ny=self.Ny,
+                               Nz=self.Nz, _geom=g, _fx=fx, _fy=fy, _fz=fz, _dv=dv)
+        self._mg = KappaMultigrid(view)
+        return self._mg
+
+    def _anchored_phase(self) -> torch.Tensor:
+        """Phase indices (natural layout, uint8) with conductive voxels of clusters that touch
+        neither x-face set to 0 (tf_anchored_phase)."""
+        cached = getattr(self, "_phase_anchored", None)
+        if cached is not None:
+            return cached
+        n = self.batch_size * self.Nx * self.Ny * self.Nz
+        dev = self.device
+        labels = torch.empty(n, dtype=torch.int32, device=dev)
+        flags = torch.empty(n, dtype=torch.uint8, device=dev)
+        phase = torch.empty(n, dtype=torch.uint8, device=dev)
+        check(self._lib.tf_anchored_phase(self.batch_size, self.Nx, self.Ny, self.Nz, self._periodic,
+                                          _ptr(self._phase_dev), self._conductive_table(), _ptr(labels),
+                                          _ptr(flags), _ptr(phase), _ptr(self._err), self._stream()),
+              "tf_anchored_phase")
+        del labels, flags
+        if int(self._err.item()):
+            self._err.zero_()
+            raise _capi.TfError(_capi.TF_ERR_TIMEOUT, "tf_anchored_phase (device)")
+        self._phase_anchored = phase
+        return phase
 
     def _anchored_code(self) -> torch.Tensor:
         """Codes of the system the FP64 refinement solves: conductive voxels of clusters that touch
@@ -254,23 +333,11 @@ class SORSolver:
         cached = getattr(self, "_code_anchored", None)
         if cached is not None:
             return cached
-        n = self.batch_size * self.Nx * self.Ny * self.Nz
-        dev = self.device
-        labels = torch.empty(n, dtype=torch.int32, device=dev)
-        flags = torch.empty(n, dtype=torch.uint8, device=dev)
-        phase = torch.empty(n, dtype=torch.uint8, device=dev)
-        st = self._stream()
-        check(self._lib.tf_anchored_phase(self.batch_size, self.Nx, self.Ny, self.Nz, self._periodic,
-                                          _ptr(self._phase_dev), self._conductive_table(), _ptr(labels),
-                                          _ptr(flags), _ptr(phase), _ptr(self._err), st), "tf_anchored_phase")
-        del labels, flags
+        phase = self._anchored_phase()
         code = torch.empty_like(self._code)
-        scratch = torch.empty(self._geom.field_elems, dtype=torch.float32, device=dev)
+        scratch = torch.empty(self._geom.field_elems, dtype=torch.float32, device=self.device)
         check(self._lib.tf_pack(C.byref(self._geom), C.byref(self._op), _ptr(phase), _ptr(self._profile_dev),
-                                _ptr(code), _ptr(scratch), st), "tf_pack")
-        if int(self._err.item()):
-            self._err.zero_()
-            raise _capi.TfError(_capi.TF_ERR_TIMEOUT, "tf_anchored_phase (device)")
+                                _ptr(code), _ptr(scratch), self._stream()), "tf_pack")
         self._code_anchored = code
         return code
 
@@ -486,10 +553,11 @@ def relative_residual(r2: torch.Tensor, b2: torch.Tensor) -> float:
 
 
 def refine_field(lib, g: TfGeom, op: TfOperator, cur: torch.Tensor, code: torch.Tensor, err: torch.Tensor, stream,
-                 batch: int, tol: float, max_outer: int, n_inner: int, omega: float | None = None):
+                 batch: int, tol: float, max_outer: int, n_inner: int, omega: float | None = None, solve_e=None):
     """FP64 defect correction of the float32 field `cur` (updated in place with the rounding of
     the result); returns the float64 field and the max-over-volumes relative residual history.
-    omega: over-relaxation of the correction sweeps (default: the solve's own)."""
+    omega: over-relaxation of the correction sweeps (default: the solve's own). solve_e(e, r):
+    another inner solve of A e = r (float32 buffers; may overwrite r) instead of the sweeps."""
     gp = C.byref(g)
     op0 = TfOperator.from_buffer_copy(op)
     op0.ghost_lo = op0.ghost_hi = 0.0
@@ -511,6 +579,10 @@ def refine_field(lib, g: TfGeom, op: TfOperator, cur: torch.Tensor, code: torch.
         hist.append(rel)
         if rel < tol or outer == max_outer:
             break
+        if solve_e is not None:
+            solve_e(ea, rhs)
+            check(lib.tf_axpy_f64(gp, _ptr(c64), _ptr(ea), stream), "tf_axpy_f64")
+            continue
         ea.zero_()
         in_b = C.c_int(0)
         check(lib.tf_advance_rhs(gp, C.byref(op0), _ptr(ea), _ptr(eb), _ptr(code), _ptr(rhs), 0, n_inner, _ptr(err),
@@ -819,6 +891,14 @@ class MultiPhaseSolver(ThroughTransportSolver):
         cond = np.isin(self.cpu_img, np.array(self.conductive_labels, dtype=np.float64)) \
             if self.conductive_labels else np.zeros(self.cpu_img.shape, dtype=bool)
         return idx, cond
+
+    def _phase_conductivities(self) -> np.ndarray:
+        """float32 diffusivity of every packed phase index (0 unused, i = label i-1), the values
+        of the face table."""
+        t = np.zeros(256, dtype=np.float32)
+        for a, lbl in enumerate(self._labels, start=1):
+            t[a] = F32(self.Ds[int(lbl)] if int(lbl) in self.Ds else self.Ds.get(lbl, 0.0))
+        return t
 
     def _operator(self, omega):
         op = super()._operator(omega)
