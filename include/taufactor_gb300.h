@@ -385,6 +385,28 @@ int tf_kappa_gradient(const tf_geom* g, const tf_operator* op, const double* fie
 /* double field layout -> natural [batch][nx][ny][nz]. */
 int tf_split_to_natural_f64(const tf_geom* g, const double* split_dev, double* natural_dev, void* stream);
 
+/* The float64 coefficients (coeff_f64 = 1) packed once per kappa field, in the layout of
+ * tf_kappa_faces but double: fx_dev batch * (nx + 1) planes (planes 0 and nx: the Dirichlet faces
+ * kappa), fy_dev / fz_dev the +y / +z face of every cell, div_dev the diagonal (0 for a voxel
+ * outside the system). Each face costs a float64 division; the three functions below read them
+ * instead (no reference counterpart: the float64 steps of the FP64 correction and adjoint). */
+int tf_kappa_faces_f64(const tf_geom* g, const float* kappa_split_dev, double* fx_dev, double* fy_dev, double* fz_dev,
+                       double* div_dev, void* stream);
+/* tf_kappa_residual_f64 with coeff_f64 = 1 from the packed faces (float64 fused multiply-adds:
+ * the same r to a few float64 roundings). */
+int tf_kappa_residual_faces_f64(const tf_geom* g, const tf_operator* op, const double* field64_dev,
+                                const double* fx_dev, const double* fy_dev, const double* fz_dev,
+                                const double* div_dev, const double* b64_dev, float* rhs_dev, double* r2_sum_dev,
+                                double* b2_sum_dev, void* stream);
+/* tf_kappa_layer_sums on a double field with coeff_f64 = 1, from the packed x faces. */
+int tf_kappa_layer_sums_faces_f64(const tf_geom* g, const double* field64_dev, const double* fx_dev,
+                                  double* flux_sum_dev, double* c_sum_dev, void* stream);
+/* tf_kappa_gradient from the packed faces: d face / d kappa_u = face^2 / (2 kappa_u^2). */
+int tf_kappa_gradient_faces_f64(const tf_geom* g, const tf_operator* op, const double* field64_dev,
+                                const double* lambda64_dev, const float* kappa_split_dev, const double* fx_dev,
+                                const double* fy_dev, const double* fz_dev, double* grad_dev, double scale,
+                                double bc_lo, double bc_hi, void* stream);
+
 /* ---- Multigrid-preconditioned conjugate gradients for the correction solve A e = r ---------
  * No reference counterpart: the reference solves only by red-black SOR (taufactor.py:156-191).
  * These serve the float32 inner solve of the FP64 defect correction (KappaSolver). A level is a

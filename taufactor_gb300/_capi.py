@@ -30,7 +30,8 @@ EXPORTS = (
     "tf_impedance_pack", "tf_impedance_fill", "tf_impedance_sweep", "tf_impedance_metrics",
     "tf_batch_advance_tile", "tf_batch_advance_rhs_tile", "tf_label_stats", "tf_anchored_phase",
     "tf_kappa_stats", "tf_mg_coarsen", "tf_mg_restrict", "tf_mg_prolong", "tf_mg_apply", "tf_mg_dot",
-    "tf_pcg_update_xr", "tf_pcg_update_p",
+    "tf_pcg_update_xr", "tf_pcg_update_p", "tf_kappa_faces_f64", "tf_kappa_residual_faces_f64",
+    "tf_kappa_layer_sums_faces_f64", "tf_kappa_gradient_faces_f64",
 )
 TF_IMP_TABLE = 56
 TF_BATCH_ACTIVE, TF_BATCH_CONVERGED, TF_BATCH_NEEDS_HOST = 0, 1, 2
@@ -136,6 +137,11 @@ def load():
         "tf_mg_dot": (i32, [G, vp, vp, vp, vp, vp, vp, vp]),
         "tf_pcg_update_xr": (i32, [G, vp, vp, vp, vp, vp, vp, vp]),
         "tf_pcg_update_p": (i32, [G, vp, vp, vp, vp, vp]),
+        "tf_kappa_faces_f64": (i32, [G, vp, vp, vp, vp, vp, vp]),
+        "tf_kappa_residual_faces_f64": (i32, [G, O, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
+        "tf_kappa_layer_sums_faces_f64": (i32, [G, vp, vp, vp, vp, vp]),
+        "tf_kappa_gradient_faces_f64": (i32, [G, O, vp, vp, vp, vp, vp, vp, vp, C.c_double, C.c_double, C.c_double,
+                                              vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)

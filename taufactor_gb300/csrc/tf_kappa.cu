@@ -189,8 +189,8 @@ __global__ void __launch_bounds__(256) k_kappa_sweep4(float* __restrict__ c, con
     const Geo& g = a.g;
     const int gmax = (half_len(g.NZ, 0) + 3) >> 2;
     const int gi = blockIdx.x * blockDim.x + threadIdx.x;
-    if (gi >= gmax) return;
-    const int y = blockIdx.y;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;  // rows of the plane across the block
+    if (gi >= gmax || y >= g.NY) return;
     const int bx = blockIdx.z;  // b * NX + x
     const int x = bx % g.NX, b = bx / g.NX;
     const int q = (x + y + colour) & 1;
@@ -428,6 +428,227 @@ __global__ void k_kappa_grad(const double* __restrict__ c64, const double* __res
     grad[(long long)blockIdx.y * n + i] = gr;
 }
 
+// ---------------------------------------------------------------- packed float64 faces
+// The float64 faces of the FP64 steps (coeff_f64 = 1) in the layout of k_kappa_face_pack,
+// computed once per kappa field: each face 2ab/(a+b) costs a float64 division, which GB300's
+// FP64 pipe makes the bound of every step that recomputes them (six per voxel per residual).
+//   fx [b][x'][plane] (x' = 0..NX; x' = 0 and NX: the Dirichlet faces kappa of planes 0, NX-1),
+//   fy, fz: the +y / +z face of every padded position; k_kappa_diag64 then writes dv, the
+//   diagonal (0 outside the system).
+__global__ void k_kappa_face_pack64(const float* __restrict__ kp, double* __restrict__ fx, double* __restrict__ fy,
+                                    double* __restrict__ fz, double* __restrict__ dv, const Geo g) {
+    const int pos = blockIdx.x * blockDim.x + threadIdx.x;  // q * ZH + jp
+    if (pos >= 2 * g.ZH) return;
+    const int Y = blockIdx.y;
+    const int bx = blockIdx.z;  // b * NX + x
+    const int x = bx % g.NX, b = bx / g.NX;
+    const int q = pos >= g.ZH ? 1 : 0;
+    const int jp = pos - q * g.ZH;
+    const long long o = (long long)bx * g.plane_f + (long long)Y * g.row_f + pos;
+    const double k = kp[o];
+    fy[o] = Y + 1 < g.YP ? hface64(k, kp[o + g.row_f]) : 0.0;
+    const long long on = q == 0 ? o + g.ZH : (jp + 1 < g.ZH ? o - g.ZH + 1 : -1);
+    fz[o] = on >= 0 ? hface64(k, kp[on]) : 0.0;
+    const long long fxo = ((long long)b * (g.NX + 1) + x) * g.plane_f + (long long)Y * g.row_f + pos;
+    fx[fxo + g.plane_f] = x + 1 < g.NX ? hface64(k, kp[o + g.plane_f]) : k;
+    if (x == 0) fx[fxo] = k;
+}
+
+// The diagonal of the packed float64 faces: the six faces of kappa_faces_fp64<true> read back
+// (hface64 is symmetric, so a face packed at the neighbour is the same float64), summed in its
+// order, the Dirichlet faces once more; 0 outside the system. One thread per padded position.
+__global__ void k_kappa_diag64(const double* __restrict__ fx, const double* __restrict__ fy,
+                               const double* __restrict__ fz, double* __restrict__ dv, const Geo g) {
+    const int pos = blockIdx.x * blockDim.x + threadIdx.x;  // q * ZH + jp
+    if (pos >= 2 * g.ZH) return;
+    const int Y = blockIdx.y;
+    const int bx = blockIdx.z;  // b * NX + x
+    const int x = bx % g.NX, b = bx / g.NX;
+    const int q = pos >= g.ZH ? 1 : 0;
+    const int jp = pos - q * g.ZH;
+    const long long o = (long long)bx * g.plane_f + (long long)Y * g.row_f + pos;
+    const int y = Y - HY, z = 2 * (jp - HJ) + q;
+    double d = 0.0;
+    if (y >= 0 && y < g.NY && jp >= HJ && z < g.NZ) {
+        const long long fxo = ((long long)b * (g.NX + 1) + x) * g.plane_f + (long long)Y * g.row_f + pos;
+        const KView v{g};
+        const long long b0 = (long long)b * g.vol_f;
+        const double xm = fx[fxo], xp = fx[fxo + g.plane_f];
+        const double ym = fy[b0 + v.off(x, y - 1, z)], yp = fy[o];
+        const double zm = fz[b0 + v.off(x, y, z - 1)], zp = fz[o];
+        d = xm + xp + ym + yp + zm + zp;
+        if (x == 0) d += xm;
+        if (x == g.NX - 1) d += xp;
+        if (!(d > 0.0)) d = 0.0;
+    }
+    dv[o] = d;
+}
+
+// k_kappa_residual<true> from the packed float64 faces with fused multiply-adds (the same r to
+// a few float64 roundings); 1024 threads per plane.
+__global__ void __launch_bounds__(1024, 1) k_kappa_residual_p64(const double* __restrict__ c64,
+                                                            const double* __restrict__ fx,
+                                                            const double* __restrict__ fy,
+                                                            const double* __restrict__ fz,
+                                                            const double* __restrict__ dv,
+                                                            const double* __restrict__ bsrc, float* __restrict__ r32,
+                                                            double* __restrict__ r2, double* __restrict__ b2,
+                                                            const Geo g, float glo, float ghi) {
+    __shared__ double red[2][32];
+    const KView v{g};
+    const int x = blockIdx.x, b = blockIdx.y;
+    const long long b0 = (long long)b * g.vol_f;
+    const long long fx0 = ((long long)b * (g.NX + 1) + x) * g.plane_f - (long long)x * g.plane_f;  // + v.off
+    const double* cb = c64 + b0;
+    double rs = 0.0, bs = 0.0;
+    // warp w takes rows y = w, w + 32, ...; its lanes walk z (no index division)
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int y = wid; y < g.NY; y += nw)
+        for (int z = lane; z < g.NZ; z += 32) {
+            const long long o = v.off(x, y, z);
+            const double div = dv[b0 + o];
+            double res = 0.0, rhs = 0.0;
+            if (div > 0.0) {
+                // fused multiply-adds: GB300's FP64 pipe (2 operations per SM per clock) bounds
+                // this kernel, and each fma halves the operations of a product and a sum
+                const double xm = fx[fx0 + o], xp = fx[fx0 + o + g.plane_f];
+                const long long oym = v.off(x, y - 1, z), ozm = v.off(x, y, z - 1);
+                double s = fy[b0 + o] * cb[v.off(x, y + 1, z)];
+                s = fma(fy[b0 + oym], cb[oym], s);
+                s = fma(fz[b0 + o], cb[v.off(x, y, z + 1)], s);
+                s = fma(fz[b0 + ozm], cb[ozm], s);
+                if (x > 0) s = fma(xm, cb[o - g.plane_f], s);
+                else if (!bsrc) rhs = xm * glo;
+                if (x + 1 < g.NX) s = fma(xp, cb[o + g.plane_f], s);
+                else if (!bsrc) rhs = fma(xp, (double)ghi, rhs);
+                if (bsrc) rhs = bsrc[b0 + o];
+                res = fma(-div, cb[o], rhs + s);
+            }
+            r32[b0 + o] = (float)res;
+            rs = fma(res, res, rs);
+            bs = fma(rhs, rhs, bs);
+        }
+    for (int s = 16; s > 0; s >>= 1) {
+        rs += __shfl_xor_sync(0xffffffffu, rs, s);
+        bs += __shfl_xor_sync(0xffffffffu, bs, s);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        red[0][threadIdx.x >> 5] = rs;
+        red[1][threadIdx.x >> 5] = bs;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double p = 0.0, q = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            p += red[0][w];
+            q += red[1][w];
+        }
+        r2[(long long)b * g.NX + x] = p;
+        b2[(long long)b * g.NX + x] = q;
+    }
+}
+
+// k_kappa_layer_sums<double, true> from the packed float64 x faces (same bits).
+__global__ void __launch_bounds__(1024, 1) k_kappa_layer_sums_p64(const double* __restrict__ c,
+                                                              const double* __restrict__ fx,
+                                                              double* __restrict__ flux, double* __restrict__ csum,
+                                                              const Geo g) {
+    __shared__ double red[2][32];
+    const KView v{g};
+    const int x = blockIdx.x, b = blockIdx.y;
+    const long long b0 = (long long)b * g.vol_f;
+    const long long fx1 = ((long long)b * (g.NX + 1) + x + 1) * g.plane_f - (long long)x * g.plane_f;  // + v.off
+    const bool has_flux = x + 1 < g.NX;
+    double fs = 0.0, cs = 0.0;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (int y = wid; y < g.NY; y += nw)
+        for (int z = lane; z < g.NZ; z += 32) {
+            const long long o = v.off(x, y, z);
+            const double a = c[b0 + o];
+            cs += a;
+            if (has_flux) fs += fx[fx1 + o] * (c[b0 + o + g.plane_f] - a);
+        }
+    for (int s = 16; s > 0; s >>= 1) {
+        fs += __shfl_xor_sync(0xffffffffu, fs, s);
+        cs += __shfl_xor_sync(0xffffffffu, cs, s);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        red[0][threadIdx.x >> 5] = fs;
+        red[1][threadIdx.x >> 5] = cs;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double p = 0.0, q = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+            p += red[0][w];
+            q += red[1][w];
+        }
+        if (has_flux) flux[(long long)b * (g.NX - 1) + x] = p;
+        csum[(long long)b * g.NX + x] = q;
+    }
+}
+
+// dJ/dkappa per voxel (k_kappa_grad's formula) from the packed float64 faces: d face / d k_u
+// = 2 k_w^2 / (k_u + k_w)^2 = face^2 / (2 k_u^2), one division per voxel instead of one per face
+// (the original form where k_u = 0). Out: natural layout [b][x][y][z] float64.
+__global__ void k_kappa_grad_p64(const double* __restrict__ c64, const double* __restrict__ lam,
+                                 const float* __restrict__ kp, const double* __restrict__ fx,
+                                 const double* __restrict__ fy, const double* __restrict__ fz,
+                                 double* __restrict__ grad, const Geo g, int periodic, double K, double bc_lo,
+                                 double bc_hi) {
+    const KView v{g};
+    const long long n = (long long)g.NX * g.NY * g.NZ;
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int x = (int)(i / ((long long)g.NY * g.NZ));
+    const int rem = (int)(i - (long long)x * g.NY * g.NZ);
+    const int y = rem / g.NZ, z = rem - y * g.NZ;
+    const long long b0 = (long long)blockIdx.y * g.vol_f;
+    const long long fxb = ((long long)blockIdx.y * (g.NX + 1)) * g.plane_f;
+    const long long o = v.off(x, y, z);
+    const double ku = kp[b0 + o], cu = c64[b0 + o], lu = lam[b0 + o];
+    const double inv = ku > 0.0 ? 1.0 / (2.0 * ku * ku) : 0.0;
+    // d face / d k_u from the face (ku > 0) or from k_w (ku = 0: 2 k_w^2 / k_w^2 = 2 if k_w > 0)
+    auto dface = [&](double face, double kw) { return ku > 0.0 ? face * face * inv : dface_da(ku, kw); };
+    double gr = 0.0;
+    if (x > 0) {
+        const long long w = o - g.plane_f;
+        const double cw = c64[b0 + w], lw = lam[b0 + w];
+        const double dj = K * (cu - cw) - (lu - lw) * (cu - cw);
+        gr += dj * dface(fx[fxb + o], kp[b0 + w]);
+    } else {
+        gr += 2.0 * lu * (bc_lo - cu);
+    }
+    if (x + 1 < g.NX) {
+        const long long w = o + g.plane_f;
+        const double cw = c64[b0 + w], lw = lam[b0 + w];
+        const double dj = K * (cw - cu) - (lu - lw) * (cu - cw);
+        gr += dj * dface(fx[fxb + o + g.plane_f], kp[b0 + w]);
+    } else {
+        gr += 2.0 * lu * (bc_hi - cu);
+    }
+    // y and z faces: packed at the lower cell of each pair; ghost positions hold the wrapped
+    // faces (periodic) or 0 (closed, derivative 0)
+    const int dy[4] = {1, -1, 0, 0}, dz[4] = {0, 0, 1, -1};
+    for (int k = 0; k < 4; ++k) {
+        int yy = y + dy[k], zq = z + dz[k];
+        if (yy < 0 || yy >= g.NY) {
+            if (!(periodic & TF_PERIODIC_Y)) continue;
+            yy = wrap(yy, g.NY);
+        }
+        if (zq < 0 || zq >= g.NZ) {
+            if (!(periodic & TF_PERIODIC_Z)) continue;
+            zq = wrap(zq, g.NZ);
+        }
+        const double face = k == 0 ? fy[b0 + o] : k == 1 ? fy[b0 + v.off(x, y - 1, z)]
+                          : k == 2 ? fz[b0 + o] : fz[b0 + v.off(x, y, z - 1)];
+        const long long w = v.off(x, yy, zq);
+        const double kw = kp[b0 + w], cw = c64[b0 + w], lw = lam[b0 + w];
+        gr += -(lu - lw) * (cu - cw) * dface(face, kw);
+    }
+    grad[(long long)blockIdx.y * n + i] = gr;
+}
+
 }  // namespace tf
 
 // ------------------------------------------------------------------------------ host side
@@ -535,8 +756,9 @@ int tf_kappa_advance_faces(const tf_geom* g, const tf_operator* op, float* field
     cudaStream_t st = (cudaStream_t)stream;
     const Geo geo = make_geo(*g);
     const int gmax = (half_len(g->nz, 0) + 3) >> 2;
-    const int bs = gmax >= 128 ? 128 : (gmax >= 32 ? 64 : 32);
-    dim3 grid((gmax + bs - 1) / bs, g->ny, g->batch * g->nx);
+    // a warp per 32 float4 groups of one half-row, 8 rows per block
+    const dim3 bs(32, 8);
+    dim3 grid((gmax + 31) / 32, (g->ny + 7) / 8, g->batch * g->nx);
     int colour = first_colour & 1;
     for (int i = 0; i < n_half; ++i, colour ^= 1) {
         SweepArgs a = make_args(geo, *op, field_dev, colour, 1, nullptr);
@@ -623,6 +845,62 @@ int tf_split_to_natural_f64(const tf_geom* g, const double* split_dev, double* n
     const long long n = (long long)g->nx * g->ny * g->nz;
     k_split_to_natural<<<dim3((unsigned)((n + 255) / 256), g->batch), 256, 0, (cudaStream_t)stream>>>(
         split_dev, natural_dev, geo);
+    note_launch();
+    return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
+}
+
+int tf_kappa_faces_f64(const tf_geom* g, const float* kappa_split_dev, double* fx_dev, double* fy_dev, double* fz_dev,
+                       double* div_dev, void* stream) {
+    if (!g || !kappa_split_dev || !fx_dev || !fy_dev || !fz_dev || !div_dev) return TF_ERR_ARG;
+    if ((long long)g->batch * g->nx > 65535 || g->yp > 65535) return TF_ERR_UNSUPPORTED;
+    const Geo geo = make_geo(*g);
+    dim3 grid((2 * g->zh + 127) / 128, g->yp, g->batch * g->nx);
+    k_kappa_face_pack64<<<grid, 128, 0, (cudaStream_t)stream>>>(kappa_split_dev, fx_dev, fy_dev, fz_dev, div_dev, geo);
+    note_launch();
+    if (cudaGetLastError() != cudaSuccess) return TF_ERR_CUDA;
+    k_kappa_diag64<<<grid, 128, 0, (cudaStream_t)stream>>>(fx_dev, fy_dev, fz_dev, div_dev, geo);
+    note_launch();
+    return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
+}
+
+int tf_kappa_residual_faces_f64(const tf_geom* g, const tf_operator* op, const double* field64_dev,
+                                const double* fx_dev, const double* fy_dev, const double* fz_dev,
+                                const double* div_dev, const double* b64_dev, float* rhs_dev, double* r2_sum_dev,
+                                double* b2_sum_dev, void* stream) {
+    if (!g || !op || !field64_dev || !fx_dev || !fy_dev || !fz_dev || !div_dev || !rhs_dev || !r2_sum_dev ||
+        !b2_sum_dev)
+        return TF_ERR_ARG;
+    const Geo geo = make_geo(*g);
+    k_kappa_residual_p64<<<dim3(g->nx, g->batch), 1024, 0, (cudaStream_t)stream>>>(
+        field64_dev, fx_dev, fy_dev, fz_dev, div_dev, b64_dev, rhs_dev, r2_sum_dev, b2_sum_dev, geo, op->ghost_lo,
+        op->ghost_hi);
+    note_launch();
+    if (cudaGetLastError() != cudaSuccess) return TF_ERR_CUDA;
+    return op->periodic ? refresh_ghosts(*g, op->periodic, rhs_dev, (cudaStream_t)stream) : TF_OK;
+}
+
+int tf_kappa_layer_sums_faces_f64(const tf_geom* g, const double* field64_dev, const double* fx_dev,
+                                  double* flux_sum_dev, double* c_sum_dev, void* stream) {
+    if (!g || !field64_dev || !fx_dev || !c_sum_dev || (g->nx > 1 && !flux_sum_dev)) return TF_ERR_ARG;
+    const Geo geo = make_geo(*g);
+    k_kappa_layer_sums_p64<<<dim3(g->nx, g->batch), 1024, 0, (cudaStream_t)stream>>>(field64_dev, fx_dev,
+                                                                                     flux_sum_dev, c_sum_dev, geo);
+    note_launch();
+    return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
+}
+
+int tf_kappa_gradient_faces_f64(const tf_geom* g, const tf_operator* op, const double* field64_dev,
+                                const double* lambda64_dev, const float* kappa_split_dev, const double* fx_dev,
+                                const double* fy_dev, const double* fz_dev, double* grad_dev, double scale,
+                                double bc_lo, double bc_hi, void* stream) {
+    if (!g || !op || !field64_dev || !lambda64_dev || !kappa_split_dev || !fx_dev || !fy_dev || !fz_dev || !grad_dev)
+        return TF_ERR_ARG;
+    const Geo geo = make_geo(*g);
+    const long long n = (long long)g->nx * g->ny * g->nz;
+    const dim3 grid((unsigned)((n + 255) / 256), g->batch);
+    k_kappa_grad_p64<<<grid, 256, 0, (cudaStream_t)stream>>>(field64_dev, lambda64_dev, kappa_split_dev, fx_dev,
+                                                             fy_dev, fz_dev, grad_dev, geo, op->periodic, scale, bc_lo,
+                                                             bc_hi);
     note_launch();
     return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
 }

@@ -145,19 +145,17 @@ __global__ void k_mg_coarsen(const float* __restrict__ fx, const float* __restri
     cdv[o] = d;
 }
 
-// One thread per interior cell of the coarse level (blockIdx.y = volume): the sum over the
-// aggregate of the fine residual, children in a fixed order.
-__global__ void __launch_bounds__(256) k_mg_restrict(const float* __restrict__ e, const float* __restrict__ rhs,
+// One thread per interior cell of the coarse level: the sum over the aggregate of the fine
+// residual, children in a fixed order.
+__global__ void __launch_bounds__(128) k_mg_restrict(const float* __restrict__ e, const float* __restrict__ rhs,
                                                      const float* __restrict__ fx, const float* __restrict__ fy,
                                                      const float* __restrict__ fz, const float* __restrict__ dv,
                                                      const Geo f, float* __restrict__ rc, const Geo c, const Shift sh) {
-    const long long n = (long long)c.NX * c.NY * c.NZ;
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int b = blockIdx.y;
-    const int xc = (int)(i / ((long long)c.NY * c.NZ));
-    const int rem = (int)(i - (long long)xc * c.NY * c.NZ);
-    const int yc = rem / c.NZ, zc = rem - yc * c.NZ;
+    // grid (z blocks, y, b * NX + x) of the coarse level: no index division
+    const int zc = blockIdx.x * blockDim.x + threadIdx.x;
+    if (zc >= c.NZ) return;
+    const int yc = blockIdx.y;
+    const int xc = blockIdx.z % c.NX, b = blockIdx.z / c.NX;
     const int x0 = xc << sh.x, y0 = yc << sh.y, z0 = zc << sh.z;
     const int xl = sh.x && x0 + 1 < f.NX ? x0 + 1 : x0;
     const int yl = sh.y && y0 + 1 < f.NY ? y0 + 1 : y0;
@@ -170,53 +168,118 @@ __global__ void __launch_bounds__(256) k_mg_restrict(const float* __restrict__ e
 }
 
 // One thread per interior cell of the fine level: e += coarse e of its aggregate.
-__global__ void __launch_bounds__(256) k_mg_prolong(const float* __restrict__ ec, const Geo c, float* __restrict__ e,
+__global__ void __launch_bounds__(128) k_mg_prolong(const float* __restrict__ ec, const Geo c, float* __restrict__ e,
                                                     const Geo f, const Shift sh) {
-    const long long n = (long long)f.NX * f.NY * f.NZ;
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int b = blockIdx.y;
-    const int x = (int)(i / ((long long)f.NY * f.NZ));
-    const int rem = (int)(i - (long long)x * f.NY * f.NZ);
-    const int y = rem / f.NZ, z = rem - y * f.NZ;
+    // grid (z blocks, y, b * NX + x) of the fine level
+    const int z = blockIdx.x * blockDim.x + threadIdx.x;
+    if (z >= f.NZ) return;
+    const int y = blockIdx.y;
+    const int x = blockIdx.z % f.NX, b = blockIdx.z / f.NX;
     e[cell(f, b, x, y, z)] += ec[cell(c, b, x >> sh.x, y >> sh.y, z >> sh.z)];
 }
 
-// out = A in on interior cells (A in = factor * in - weighted neighbour sum, Dirichlet ghosts 0).
+// out = A in on interior cells (A in = factor * in - weighted neighbour sum, Dirichlet ghosts 0):
+// one thread per float4 group of a half-row (blockIdx.y: row groups of 8, threadIdx.y the row;
+// blockIdx.z = b * NX + x), both half-rows; 0 where the factor is not finite.
 __global__ void __launch_bounds__(256) k_mg_apply(const float* __restrict__ in, const float* __restrict__ fx,
                                                   const float* __restrict__ fy, const float* __restrict__ fz,
                                                   const float* __restrict__ dv, float* __restrict__ out, const Geo g) {
-    const long long n = (long long)g.NX * g.NY * g.NZ;
-    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const int b = blockIdx.y;
-    const int x = (int)(i / ((long long)g.NY * g.NZ));
-    const int rem = (int)(i - (long long)x * g.NY * g.NZ);
-    const int y = rem / g.NZ, z = rem - y * g.NZ;
-    out[cell(g, b, x, y, z)] = -residual_at(g, b, x, y, z, in, nullptr, fx, fy, fz, dv);
-}
-
-// Per padded row (blockIdx.x = row y of plane blockIdx.y = b * NX + x): float64 sums over the
-// row's interior cells of a1*b1 and (if a2) a2*b2 -> part[2][B*NX*NY].
-__global__ void __launch_bounds__(128) k_mg_dot_rows(const float* __restrict__ a1, const float* __restrict__ b1,
-                                                     const float* __restrict__ a2, const float* __restrict__ b2,
-                                                     double* __restrict__ part, const Geo g) {
-    __shared__ double red[2][4];
-    const int y = blockIdx.x;
-    const long long bx = blockIdx.y;
-    const long long row = bx * g.plane_f + (long long)(y + HY) * g.row_f;
-    double s1 = 0.0, s2 = 0.0;
+    const int gmax = (half_len(g.NZ, 0) + 3) >> 2;
+    const int gi = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (gi >= gmax || y >= g.NY) return;
+    const int bx = blockIdx.z;
+    const int x = bx % g.NX, b = bx / g.NX;
+    const int j = 4 * gi;
+    const long long row = (long long)bx * g.plane_f + (long long)(y + HY) * g.row_f;
+    const long long fxr = ((long long)b * (g.NX + 1) + x) * g.plane_f + (long long)(y + HY) * g.row_f;
     for (int q = 0; q < 2; ++q) {
         const int nj = half_len(g.NZ, q);
-        const long long base = row + q * g.ZH + HJ;
-        for (int j = threadIdx.x; j < nj; j += blockDim.x) {
-            s1 += (double)a1[base + j] * (double)b1[base + j];
-            if (a2) s2 += (double)a2[base + j] * (double)b2[base + j];
+        if (j >= nj) continue;
+        const long long rq = row + q * g.ZH + HJ + j;        // this group
+        const long long ro = row + (q ^ 1) * g.ZH + HJ + j;  // the other half-row, same j
+        const float4 cc = ld4(in + rq);
+        const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 xp = x + 1 < g.NX ? ld4(in + rq + g.plane_f) : zero4;
+        const float4 xm = x > 0 ? ld4(in + rq - g.plane_f) : zero4;
+        const float4 yp = ld4(in + rq + g.row_f), ym = ld4(in + rq - g.row_f);
+        float4 zp, zm;
+        z_neighbours(q, ld4(in + ro), q ? in[ro + 4] : in[ro - 1], zp, zm);
+        const long long fq = fxr + q * g.ZH + HJ + j;
+        const float4 fxm = ld4(fx + fq), fxp = ld4(fx + fq + g.plane_f);
+        const float4 fyp = ld4(fy + rq), fym = ld4(fy + rq - g.row_f);
+        const float4 fzp = ld4(fz + rq);
+        float4 fzm;  // the face between z - 1 and z, stored at cell z - 1
+        if (q) {
+            fzm = ld4(fz + ro);
+        } else {
+            const float4 fo = ld4(fz + ro);
+            fzm = make_float4(fz[ro - 1], fo.x, fo.y, fo.z);
+        }
+        const float4 d = ld4(dv + rq);
+        float4 r;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            float s = comp(xp, i) * comp(fxp, i) + comp(xm, i) * comp(fxm, i);
+            s += comp(yp, i) * comp(fyp, i);
+            s += comp(ym, i) * comp(fym, i);
+            s += comp(zp, i) * comp(fzp, i);
+            s += comp(zm, i) * comp(fzm, i);
+            const float di = comp(d, i);
+            set_comp(r, i, di < kInf ? di * comp(cc, i) - s : 0.0f);
+        }
+        float* dst = out + rq;
+        if (j + 4 <= nj)
+            st4(dst, r);
+        else
+            for (int i = 0; i < nj - j; ++i) dst[i] = comp(r, i);
+    }
+}
+
+// Rows of one plane per block of the dot products (the partial sums are per block).
+constexpr int kDotRows = 16;
+
+// float64 sums over interior cells of a1*b1 and (if a2) a2*b2 for kDotRows rows (blockIdx.x)
+// of the plane blockIdx.y = b * NX + x -> part[2][B*NX*ny_blocks], float4 loads, fixed order.
+__global__ void __launch_bounds__(256) k_mg_dot_rows(const float* __restrict__ a1, const float* __restrict__ b1,
+                                                     const float* __restrict__ a2, const float* __restrict__ b2,
+                                                     double* __restrict__ part, const Geo g) {
+    __shared__ double red[2][8];
+    const long long bx = blockIdx.y;
+    const int y0 = blockIdx.x * kDotRows;
+    const int y1 = y0 + kDotRows < g.NY ? y0 + kDotRows : g.NY;
+    const int n0 = half_len(g.NZ, 0), n1 = half_len(g.NZ, 1);
+    const int g0 = (n0 + 3) >> 2, g1 = (n1 + 3) >> 2;  // float4 groups per half-row
+    const int per_row = g0 + g1;
+    const long long plane = bx * g.plane_f;
+    double s1 = 0.0, s2 = 0.0;
+    for (int k = threadIdx.x; k < (y1 - y0) * per_row; k += blockDim.x) {
+        const int r = k / per_row, gi = k - r * per_row;
+        const int q = gi >= g0 ? 1 : 0;
+        const int j = 4 * (q ? gi - g0 : gi);
+        const int nj = q ? n1 : n0;
+        const long long o = plane + (long long)(y0 + r + HY) * g.row_f + q * g.ZH + HJ + j;
+        // a group's four products summed in float32 (relative error ~1e-7, ample for the CG
+        // scalars), the groups in float64: one float64 add per group instead of eight float64
+        // operations, which would bound the kernel on GB300's FP64 pipe
+        const float4 x1 = *reinterpret_cast<const float4*>(a1 + o), w1 = *reinterpret_cast<const float4*>(b1 + o);
+        float t1 = x1.x * w1.x;
+        if (j + 1 < nj) t1 += x1.y * w1.y;
+        if (j + 2 < nj) t1 += x1.z * w1.z;
+        if (j + 3 < nj) t1 += x1.w * w1.w;
+        s1 += (double)t1;
+        if (a2) {
+            const float4 x2 = *reinterpret_cast<const float4*>(a2 + o), w2 = *reinterpret_cast<const float4*>(b2 + o);
+            float t2 = x2.x * w2.x;
+            if (j + 1 < nj) t2 += x2.y * w2.y;
+            if (j + 2 < nj) t2 += x2.z * w2.z;
+            if (j + 3 < nj) t2 += x2.w * w2.w;
+            s2 += (double)t2;
         }
     }
-    for (int s = 16; s > 0; s >>= 1) {
-        s1 += __shfl_xor_sync(0xffffffffu, s1, s);
-        s2 += __shfl_xor_sync(0xffffffffu, s2, s);
+    for (int sh = 16; sh > 0; sh >>= 1) {
+        s1 += __shfl_xor_sync(0xffffffffu, s1, sh);
+        s2 += __shfl_xor_sync(0xffffffffu, s2, sh);
     }
     if ((threadIdx.x & 31) == 0) {
         red[0][threadIdx.x >> 5] = s1;
@@ -224,24 +287,29 @@ __global__ void __launch_bounds__(128) k_mg_dot_rows(const float* __restrict__ a
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-        const long long rows = (long long)g.B * g.NX * g.NY;
-        const long long k = bx * g.NY + y;
-        part[k] = (red[0][0] + red[0][1]) + (red[0][2] + red[0][3]);
-        part[rows + k] = (red[1][0] + red[1][1]) + (red[1][2] + red[1][3]);
+        double p1 = 0.0, p2 = 0.0;
+        for (int w = 0; w < 8; ++w) {
+            p1 += red[0][w];
+            p2 += red[1][w];
+        }
+        const long long nb = (long long)g.B * g.NX * gridDim.x;
+        const long long k = bx * gridDim.x + blockIdx.x;
+        part[k] = p1;
+        part[nb + k] = p2;
     }
 }
 
-// One block per volume: out[v][b] = sum of the volume's row partials of product v, fixed order.
+// One block per volume: out[v][b] = sum of the volume's block partials of product v (nper per
+// volume), fixed order.
 __global__ void __launch_bounds__(256) k_mg_dot_sum(const double* __restrict__ part, double* __restrict__ out,
-                                                    const Geo g, int nprod) {
+                                                    const Geo g, long long nper, int nprod) {
     __shared__ double red[2][8];
     const int b = blockIdx.x;
-    const long long rows = (long long)g.B * g.NX * g.NY;
-    const long long per = (long long)g.NX * g.NY;
+    const long long nb = (long long)g.B * nper;
     for (int v = 0; v < nprod; ++v) {
-        const double* p = part + v * rows + b * per;
+        const double* p = part + v * nb + b * nper;
         double s = 0.0;
-        for (long long k = threadIdx.x; k < per; k += blockDim.x) s += p[k];
+        for (long long k = threadIdx.x; k < nper; k += blockDim.x) s += p[k];
         for (int sh = 16; sh > 0; sh >>= 1) s += __shfl_xor_sync(0xffffffffu, s, sh);
         if ((threadIdx.x & 31) == 0) red[v][threadIdx.x >> 5] = s;
     }
@@ -301,10 +369,9 @@ static bool coarse_of(const tf_geom& f, const tf_geom& c, Shift* sh) {
            axis(f.nx, c.nx, &sh->x) && axis(f.ny, c.ny, &sh->y) && axis(f.nz, c.nz, &sh->z);
 }
 
-static dim3 cell_grid(const tf_geom& g) {
-    const long long n = (long long)g.nx * g.ny * g.nz;
-    return dim3((unsigned)((n + 255) / 256), g.batch);
-}
+// (z blocks of 128, y, b * nx + x) over the interior cells of a level
+static dim3 cell_grid(const tf_geom& g) { return dim3((g.nz + 127) / 128, g.ny, g.batch * g.nx); }
+static bool cell_grid_ok(const tf_geom& g) { return (long long)g.batch * g.nx <= 65535 && g.ny <= 65535; }
 
 static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15) == 0; }
 
@@ -335,9 +402,10 @@ int tf_mg_restrict(const tf_geom* fine, const float* e_dev, const float* rhs_dev
                    float* rc_dev, void* stream) {
     if (!fine || !coarse || !e_dev || !fx_dev || !fy_dev || !fz_dev || !div_dev || !rc_dev) return TF_ERR_ARG;
     Shift sh;
-    if (!coarse_of(*fine, *coarse, &sh) || coarse->batch > 65535) return TF_ERR_ARG;
+    if (!coarse_of(*fine, *coarse, &sh)) return TF_ERR_ARG;
+    if (!cell_grid_ok(*coarse)) return TF_ERR_UNSUPPORTED;
     const Geo f = make_geo(*fine), c = make_geo(*coarse);
-    k_mg_restrict<<<cell_grid(*coarse), 256, 0, (cudaStream_t)stream>>>(e_dev, rhs_dev, fx_dev, fy_dev, fz_dev,
+    k_mg_restrict<<<cell_grid(*coarse), 128, 0, (cudaStream_t)stream>>>(e_dev, rhs_dev, fx_dev, fy_dev, fz_dev,
                                                                          div_dev, f, rc_dev, c, sh);
     note_launch();
     return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
@@ -347,10 +415,11 @@ int tf_mg_prolong(const tf_geom* coarse, const float* ec_dev, const tf_geom* fin
                   void* stream) {
     if (!fine || !coarse || !ec_dev || !e_dev) return TF_ERR_ARG;
     Shift sh;
-    if (!coarse_of(*fine, *coarse, &sh) || fine->batch > 65535) return TF_ERR_ARG;
+    if (!coarse_of(*fine, *coarse, &sh)) return TF_ERR_ARG;
+    if (!cell_grid_ok(*fine)) return TF_ERR_UNSUPPORTED;
     cudaStream_t st = (cudaStream_t)stream;
     const Geo f = make_geo(*fine), c = make_geo(*coarse);
-    k_mg_prolong<<<cell_grid(*fine), 256, 0, st>>>(ec_dev, c, e_dev, f, sh);
+    k_mg_prolong<<<cell_grid(*fine), 128, 0, st>>>(ec_dev, c, e_dev, f, sh);
     note_launch();
     if (cudaGetLastError() != cudaSuccess) return TF_ERR_CUDA;
     return periodic ? refresh_ghosts(*fine, periodic, e_dev, st) : TF_OK;
@@ -360,8 +429,14 @@ int tf_mg_apply(const tf_geom* g, const float* in_dev, const float* fx_dev, cons
                 const float* fz_dev, const float* div_dev, float* out_dev, void* stream) {
     if (!g || !in_dev || !fx_dev || !fy_dev || !fz_dev || !div_dev || !out_dev || g->batch > 65535)
         return TF_ERR_ARG;
+    if (!aligned16(in_dev) || !aligned16(fx_dev) || !aligned16(fy_dev) || !aligned16(fz_dev) || !aligned16(div_dev) ||
+        !aligned16(out_dev) || (long long)g->batch * g->nx > 65535)
+        return TF_ERR_ARG;
     const Geo geo = make_geo(*g);
-    k_mg_apply<<<cell_grid(*g), 256, 0, (cudaStream_t)stream>>>(in_dev, fx_dev, fy_dev, fz_dev, div_dev, out_dev, geo);
+    const int gmax = (half_len(g->nz, 0) + 3) >> 2;
+    const dim3 bs(32, 8);
+    const dim3 grid((gmax + 31) / 32, (g->ny + 7) / 8, g->batch * g->nx);
+    k_mg_apply<<<grid, bs, 0, (cudaStream_t)stream>>>(in_dev, fx_dev, fy_dev, fz_dev, div_dev, out_dev, geo);
     note_launch();
     return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
 }
@@ -369,14 +444,17 @@ int tf_mg_apply(const tf_geom* g, const float* in_dev, const float* fx_dev, cons
 int tf_mg_dot(const tf_geom* g, const float* a1_dev, const float* b1_dev, const float* a2_dev, const float* b2_dev,
               double* part_dev, double* out_dev, void* stream) {
     if (!g || !a1_dev || !b1_dev || !part_dev || !out_dev || (!a2_dev) != (!b2_dev)) return TF_ERR_ARG;
-    if ((long long)g->batch * g->nx > 65535 || g->ny > 2147483647 / 2) return TF_ERR_UNSUPPORTED;
+    if ((long long)g->batch * g->nx > 65535) return TF_ERR_UNSUPPORTED;
+    if (!aligned16(a1_dev) || !aligned16(b1_dev) || (a2_dev && (!aligned16(a2_dev) || !aligned16(b2_dev))))
+        return TF_ERR_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     const Geo geo = make_geo(*g);
-    dim3 grid(g->ny, g->batch * g->nx);
-    k_mg_dot_rows<<<grid, 128, 0, st>>>(a1_dev, b1_dev, a2_dev, b2_dev, part_dev, geo);
+    const int nyb = (g->ny + kDotRows - 1) / kDotRows;
+    dim3 grid(nyb, g->batch * g->nx);
+    k_mg_dot_rows<<<grid, 256, 0, st>>>(a1_dev, b1_dev, a2_dev, b2_dev, part_dev, geo);
     note_launch();
     if (cudaGetLastError() != cudaSuccess) return TF_ERR_CUDA;
-    k_mg_dot_sum<<<g->batch, 256, 0, st>>>(part_dev, out_dev, geo, a2_dev ? 2 : 1);
+    k_mg_dot_sum<<<g->batch, 256, 0, st>>>(part_dev, out_dev, geo, (long long)g->nx * nyb, a2_dev ? 2 : 1);
     note_launch();
     return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
 }

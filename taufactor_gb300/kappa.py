@@ -18,10 +18,12 @@ faces (``coefficients="f32"``, the reference's operator and what the float32 swe
 moves in steps of one float32 rounding of a face, which puts about 1e-7/h relative noise into a
 central difference of step h. The two refined D_eff differ by about 1e-7 relative.
 
-The inner solve of each FP64 correction step is either the float32 SOR sweeps
+The FP64 steps solve the anchored system of the FP64 oracle: where kappa has zeros, voxels of
+clusters that touch neither x face (no flux passes through them; their block of the operator is
+singular) are left out (kappa 0 for the float64 steps; the float32 loop keeps the reference's
+operator). The inner solve of each FP64 correction step is either the float32 SOR sweeps
 (``inner="sor"``) or conjugate gradients preconditioned by a multigrid V-cycle
-(``inner="mg"``, ``multigrid.KappaMultigrid``); ``"auto"`` (the default) takes multigrid when
-kappa > 0 everywhere, where every cluster touches the Dirichlet faces, and SOR otherwise.
+(``inner="mg"``, ``multigrid.KappaMultigrid``, the default ``"auto"``).
 ``solve(method="mg")`` skips the float32 SOR loop and runs the FP64 correction with multigrid
 inner solves from the current field (the initial profile or a warm start).
 
@@ -91,9 +93,10 @@ class KappaSolver:
             pos_h, sums_h, bad_h = pos.cpu().numpy(), sums.cpu().numpy(), int(bad.item())
         if bad_h:
             raise ValueError("kappa must be finite and >= 0")
-        # every voxel conductive: every cluster touches both x faces, A is nonsingular
+        # every voxel conductive: one cluster touching both x faces, A is nonsingular
         self.all_positive = int(pos_h.sum()) == B * X * Y * Z
         self._mg = None
+        self._ks_a = None
         self.vol_x = pos_h / float(Y * Z)
         self.D_mean = sums_h.sum(axis=1) / float(X * Y * Z)
         self.cpu_img = None  # built lazily for the percolation fallback
@@ -128,6 +131,7 @@ class KappaSolver:
             self._flux = torch.empty((self.batch_size, self.Nx - 1), dtype=torch.float64, device=self.device)
             self._csum = torch.empty((self.batch_size, self.Nx), dtype=torch.float64, device=self.device)
         self._c64 = None
+        self._f64 = None
         self.iter = 0
         self.converged = False
         self.old_tau = 0
@@ -146,10 +150,29 @@ class KappaSolver:
                                                self.iter % 2 if first_colour is None else first_colour, n,
                                                self._stream()), "tf_kappa_advance_faces")
 
+    def _faces64(self):
+        """The float64 faces and diagonal of the FP64 steps (coefficients "f64"), packed once."""
+        if self._f64 is None:
+            g = self._geom
+            plane = g.field_elems // (self.batch_size * self.Nx)
+            d = dict(dtype=torch.float64, device=self.device)
+            fx = torch.empty(self.batch_size * (self.Nx + 1) * plane, **d)
+            fy, fz, dv = (torch.empty(g.field_elems, **d) for _ in range(3))
+            check(self._lib.tf_kappa_faces_f64(C.byref(g), _ptr(self._kappa64()), _ptr(fx), _ptr(fy), _ptr(fz),
+                                               _ptr(dv), self._stream()), "tf_kappa_faces_f64")
+            self._f64 = (fx, fy, fz, dv)
+        return self._f64
+
     def _layer_means(self):
         f, is64 = (self._c64, 1) if self._c64 is not None else (self._c, 0)
-        check(self._lib.tf_kappa_layer_sums(C.byref(self._geom), _ptr(f), is64, self._coeff64 & is64, _ptr(self._ks),
-                                            _ptr(self._flux), _ptr(self._csum), self._stream()), "tf_kappa_layer_sums")
+        if is64 and self._coeff64:
+            check(self._lib.tf_kappa_layer_sums_faces_f64(C.byref(self._geom), _ptr(f), _ptr(self._faces64()[0]),
+                                                          _ptr(self._flux), _ptr(self._csum), self._stream()),
+                  "tf_kappa_layer_sums_faces_f64")
+        else:
+            check(self._lib.tf_kappa_layer_sums(C.byref(self._geom), _ptr(f), is64, self._coeff64 & is64,
+                                                _ptr(self._kappa64() if is64 else self._ks), _ptr(self._flux),
+                                                _ptr(self._csum), self._stream()), "tf_kappa_layer_sums")
         area = float(self.Ny * self.Nz)
         return self._flux.cpu().numpy() / area, self._csum.cpu().numpy() / area
 
@@ -212,16 +235,61 @@ class KappaSolver:
     def _inner(self, inner: str) -> str:
         if inner not in ("auto", "sor", "mg"):
             raise ValueError('inner must be "auto", "sor" or "mg"')
-        if inner == "auto":
-            return "mg" if self.all_positive else "sor"
-        return inner
+        return "mg" if inner == "auto" else inner
+
+    def _kappa64(self) -> torch.Tensor:
+        """kappa of the FP64 steps (split layout): the solver's own where kappa > 0 everywhere,
+        else with the voxels of clusters that touch neither x face set to 0 (tf_anchored_phase
+        on the mask kappa > 0)."""
+        if self.all_positive:
+            return self._ks
+        if self._ks_a is None:
+            B, X, Y, Z = self.batch_size, self.Nx, self.Ny, self.Nz
+            n = B * X * Y * Z
+            dev, st, lib = self.device, self._stream(), self._lib
+            mask = (self.kappa > 0).to(torch.uint8)
+            labels = torch.empty(n, dtype=torch.int32, device=dev)
+            flags = torch.empty(n, dtype=torch.uint8, device=dev)
+            keep = torch.empty(n, dtype=torch.uint8, device=dev)
+            err = torch.zeros(1, dtype=torch.int32, device=dev)
+            table = (C.c_uint8 * 256)()
+            table[1] = 1
+            pflag = (TF_PERIODIC_Y | TF_PERIODIC_Z) if self.periodic else 0
+            check(lib.tf_anchored_phase(B, X, Y, Z, pflag, _ptr(mask), table, _ptr(labels), _ptr(flags), _ptr(keep),
+                                        _ptr(err), st), "tf_anchored_phase")
+            del labels, flags
+            if int(err.item()):
+                raise _capi.TfError(_capi.TF_ERR_TIMEOUT, "tf_anchored_phase (device)")
+            kap = torch.where(keep.view(B, X, Y, Z) > 0, self.kappa, torch.zeros((), device=dev))
+            ks = torch.empty_like(self._ks)
+            scratch = torch.empty_like(self._c)
+            prof = torch.zeros(self.Nx, dtype=torch.float32, device=dev)
+            check(lib.tf_kappa_pack(C.byref(self._geom), C.byref(self._op), _ptr(kap), _ptr(prof), _ptr(ks),
+                                    _ptr(scratch), st), "tf_kappa_pack")
+            self._ks_a = ks
+        return self._ks_a
 
     def multigrid(self):
-        """The multigrid preconditioner of the inner solves (built on first use)."""
+        """The multigrid preconditioner of the inner solves (built on first use), on the
+        float32 faces of the FP64 steps' kappa."""
         if self._mg is None:
+            from types import SimpleNamespace
+
             from .multigrid import KappaMultigrid
 
-            self._mg = KappaMultigrid(self)
+            if self.all_positive:
+                view = self
+            else:
+                g = self._geom
+                plane = g.field_elems // (self.batch_size * self.Nx)
+                f32 = dict(dtype=torch.float32, device=self.device)
+                fx = torch.empty(self.batch_size * (self.Nx + 1) * plane, **f32)
+                fy, fz, dv = (torch.empty(g.field_elems, **f32) for _ in range(3))
+                check(self._lib.tf_kappa_faces(C.byref(g), _ptr(self._kappa64()), _ptr(fx), _ptr(fy), _ptr(fz),
+                                               _ptr(dv), self._stream()), "tf_kappa_faces")
+                view = SimpleNamespace(device=self.device, _op=self._op, batch_size=self.batch_size, Nx=self.Nx,
+                                       Ny=self.Ny, Nz=self.Nz, _geom=g, _fx=fx, _fy=fy, _fz=fz, _dv=dv)
+            self._mg = KappaMultigrid(view)
         return self._mg
 
     def _fp64_solve(self, x64, b64, tol, max_outer, n_inner, inner="sor", inner_rtol=1e-5):
@@ -237,9 +305,16 @@ class KappaSolver:
         b2 = torch.empty_like(r2)
         hist = []
         for outer in range(max_outer + 1):
-            check(lib.tf_kappa_residual_f64(C.byref(g), C.byref(self._op), _ptr(x64), _ptr(self._ks),
-                                            _ptr(b64) if b64 is not None else None, self._coeff64, _ptr(rhs),
-                                            _ptr(r2), _ptr(b2), st), "tf_kappa_residual_f64")
+            if self._coeff64:
+                fx, fy, fz, dv = self._faces64()
+                check(lib.tf_kappa_residual_faces_f64(C.byref(g), C.byref(self._op), _ptr(x64), _ptr(fx), _ptr(fy),
+                                                      _ptr(fz), _ptr(dv), _ptr(b64) if b64 is not None else None,
+                                                      _ptr(rhs), _ptr(r2), _ptr(b2), st),
+                      "tf_kappa_residual_faces_f64")
+            else:
+                check(lib.tf_kappa_residual_f64(C.byref(g), C.byref(self._op), _ptr(x64), _ptr(self._kappa64()),
+                                                _ptr(b64) if b64 is not None else None, 0, _ptr(rhs), _ptr(r2),
+                                                _ptr(b2), st), "tf_kappa_residual_f64")
             rel = relative_residual(r2, b2)
             hist.append(rel)
             if rel < tol or outer == max_outer:
@@ -288,8 +363,8 @@ class KappaSolver:
         with torch.cuda.device(self.device):
             g, lib, st = self._geom, self._lib, self._stream()
             dj = torch.zeros(g.field_elems, dtype=torch.float64, device=self.device)
-            check(lib.tf_kappa_adjoint_rhs(C.byref(g), _ptr(self._ks), _ptr(dj), float(scale), self._coeff64, st),
-                  "tf_kappa_adjoint_rhs")
+            check(lib.tf_kappa_adjoint_rhs(C.byref(g), _ptr(self._kappa64()), _ptr(dj), float(scale), self._coeff64,
+                                           st), "tf_kappa_adjoint_rhs")
             if lam0 is not None:
                 if lam0.numel() != g.field_elems:
                     raise ValueError("lam0 must come from a solver of the same shape")
@@ -299,9 +374,16 @@ class KappaSolver:
             self.adjoint_history = self._fp64_solve(lam, dj, tol, max_outer, n_inner, inner)
             self.lam = lam
             grad = torch.empty((self.batch_size, self.Nx, self.Ny, self.Nz), dtype=torch.float64, device=self.device)
-            check(lib.tf_kappa_gradient(C.byref(g), C.byref(self._op), _ptr(self._c64), _ptr(lam), _ptr(self._ks),
-                                        _ptr(grad), float(scale), float(self.top_bc), float(self.bot_bc), st),
-                  "tf_kappa_gradient")
+            if self._coeff64:
+                fx, fy, fz, _ = self._faces64()
+                check(lib.tf_kappa_gradient_faces_f64(C.byref(g), C.byref(self._op), _ptr(self._c64), _ptr(lam),
+                                                      _ptr(self._kappa64()), _ptr(fx), _ptr(fy), _ptr(fz), _ptr(grad),
+                                                      float(scale), float(self.top_bc), float(self.bot_bc), st),
+                      "tf_kappa_gradient_faces_f64")
+            else:
+                check(lib.tf_kappa_gradient(C.byref(g), C.byref(self._op), _ptr(self._c64), _ptr(lam),
+                                            _ptr(self._kappa64()), _ptr(grad), float(scale), float(self.top_bc),
+                                            float(self.bot_bc), st), "tf_kappa_gradient")
             torch.cuda.synchronize(self.device)
         self.timings["adjoint_s"] = timer() - t0
         return grad

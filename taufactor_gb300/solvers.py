@@ -221,7 +221,7 @@ class SORSolver:
         return autotune.tune(self, half_sweeps)
 
     def refine(self, tol: float = 1e-10, max_outer: int = 12, inner_half_sweeps: int | None = None,
-               omega: float | None = None, inner: str = "sor"):
+               omega: float | None = None, inner: str = "auto"):
         """FP64 defect correction of the current field; returns the relative residual history.
 
         Keeps the solution in float64, forms r = b - A c in float64 on the device, solves A e = r
@@ -236,10 +236,13 @@ class SORSolver:
         on a 320^3 three-label one). "mg" (binary and multiphase kinds) solves it by conjugate
         gradients preconditioned with a multigrid V-cycle on the same operator, written as
         per-voxel faces (multigrid.KappaMultigrid), to a relative residual of 1e-5; clusters that
-        touch neither x face are frozen for it (the anchored system of the FP64 oracle).
+        touch neither x face are frozen for it (the anchored system of the FP64 oracle). "auto"
+        (the default): "mg" for the binary and multiphase kinds, "sor" for the others.
         """
-        if inner not in ("sor", "mg"):
-            raise ValueError('inner must be "sor" or "mg"')
+        if inner not in ("auto", "sor", "mg"):
+            raise ValueError('inner must be "auto", "sor" or "mg"')
+        if inner == "auto":
+            inner = "mg" if self._kind in (TF_KIND_BINARY, TF_KIND_MULTIPHASE) else "sor"
         n_inner = inner_half_sweeps or max(400, 2 * (self.iter or 200))
         solve_e = None
         with torch.cuda.device(self.device):

@@ -25,7 +25,8 @@ def lib():
 def test_header_declares_exactly_the_exports(lib):
     import os
 
-    hdr = open(os.path.join(os.path.dirname(os.path.dirname(__file__)), "include", "taufactor_gb300.h")).read()
+    with open(os.path.join(os.path.dirname(os.path.dirname(__file__)), "include", "taufactor_gb300.h")) as f:
+        hdr = f.read()
     declared = set(re.findall(r"\b(tf_[a-z_0-9]+)\s*\(", hdr))
     assert declared == set(_capi.EXPORTS)
     for name in declared:
