@@ -965,6 +965,17 @@ def run_profile(args):
         torch.cuda.synchronize()
         print(f"profile workload done: impedance {args.side}^3, {args.half_sweeps} half-sweeps")
         return
+    if args.multiphase:  # MultiPhaseSolver on the three-label --side^3 volume, --half-sweeps half-sweeps
+        from taufactor_gb300.synthetic import three_phase
+
+        s = tg.MultiPhaseSolver(three_phase(args.side), {0: 0.0, 1: 1.0, 2: 0.1}, device="cuda")
+        s._advance(8)
+        torch.cuda.synchronize()
+        s._advance(args.half_sweeps)
+        s._layer_means()
+        torch.cuda.synchronize()
+        print(f"profile workload done: multiphase {args.side}^3, {args.half_sweeps} half-sweeps")
+        return
     if args.multigrid:  # KappaSolver --side^3 (C4 generator, rng 3003): one FP64 correction, multigrid PCG
         from scipy.ndimage import gaussian_filter
 
@@ -1009,6 +1020,8 @@ def main():
     ap.add_argument("--side", type=int, default=256, help="--profile: volume side")
     ap.add_argument("--half-sweeps", type=int, default=40, help="--profile: half-sweeps")
     ap.add_argument("--periodic", action="store_true", help="--profile: PeriodicSolver")
+    ap.add_argument("--multiphase", action="store_true",
+                    help="--profile: MultiPhaseSolver on the three-label --side^3 volume")
     ap.add_argument("--multigrid", action="store_true",
                     help="--profile: one multigrid-PCG FP64 correction of a --side^3 kappa field")
     ap.add_argument("--impedance", action="store_true", help="--profile: ImpedanceSolver on one volume")

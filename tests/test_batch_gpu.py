@@ -164,3 +164,20 @@ def test_device_split_equals_one_batch():
     for a, b in zip(one, split):
         assert a.iter == b.iter
         assert np.array_equal(a.D_eff, b.D_eff) and np.array_equal(a.tau, b.tau)
+
+
+def test_batch_matches_the_oracle_directly():
+    """The batched solve against the oracle itself (not through the single-volume solver):
+    the reference's iteration count and D_eff (float32 sweeps, float64 layer means), binary and
+    periodic volumes of three shapes in one batch."""
+    from oracle.sor import OracleSolve
+
+    shapes = [(20, 16, 24), (16, 24, 20), (24, 20, 16)]
+    vols = [blurred_noise(s, 1.5, 0.6, 300 + i) for i, s in enumerate(shapes)]
+    periodic = [False, True, False]
+    res = tg.BatchSolve(vols, periodic=periodic).solve(conv_crit=1e-3)
+    for v, (img, per) in enumerate(zip(vols, periodic)):
+        o = OracleSolve(img, kind="periodic" if per else "binary")
+        o.solve(conv_crit=1e-3)
+        assert res[v].iter == o.iter, (v, res[v].iter, o.iter)
+        np.testing.assert_allclose(res[v].D_eff, o.D_eff, rtol=1e-6)
