@@ -97,6 +97,7 @@ class KappaSolver:
         self.all_positive = int(pos_h.sum()) == B * X * Y * Z
         self._mg = None
         self._ks_a = None
+        self.inner_fallback = False  # set when a multigrid inner solve failed and SOR took over
         self.vol_x = pos_h / float(Y * Z)
         self.D_mean = sums_h.sum(axis=1) / float(X * Y * Z)
         self.cpu_img = None  # built lazily for the percolation fallback
@@ -320,7 +321,13 @@ class KappaSolver:
             if rel < tol or outer == max_outer:
                 break
             if inner == "mg":
-                self.multigrid().solve(e, rhs, rtol=inner_rtol, max_iter=max(50, n_inner // 4))
+                _, rel_in = self.multigrid().solve(e, rhs, rtol=inner_rtol, max_iter=max(50, n_inner // 4))
+                if not (np.all(np.isfinite(rel_in)) and rel_in.max() < 0.5):
+                    # multigrid made no progress on this system: drop this correction and take
+                    # the SOR sweeps from here on (the residual is formed again from x64)
+                    inner = "sor"
+                    self.inner_fallback = True
+                    continue
             else:
                 e.zero_()
                 self._advance(n_inner, e, rhs=rhs, op=op0, first_colour=0)

@@ -243,6 +243,7 @@ class SORSolver:
             raise ValueError('inner must be "auto", "sor" or "mg"')
         if inner == "auto":
             inner = "mg" if self._kind in (TF_KIND_BINARY, TF_KIND_MULTIPHASE) else "sor"
+        self.inner_fallback = False  # set when a multigrid inner solve failed and SOR took over
         n_inner = inner_half_sweeps or max(400, 2 * (self.iter or 200))
         solve_e = None
         with torch.cuda.device(self.device):
@@ -251,7 +252,10 @@ class SORSolver:
                 code = self._anchored_code()
 
                 def solve_e(e, r):
-                    mg.solve(e, r, rtol=1e-5, max_iter=max(50, n_inner // 4))
+                    _, rel_in = mg.solve(e, r, rtol=1e-5, max_iter=max(50, n_inner // 4))
+                    ok = bool(np.all(np.isfinite(rel_in)) and rel_in.max() < 0.5)
+                    self.inner_fallback = self.inner_fallback or not ok
+                    return ok
             else:
                 code = self._code if self._kind == TF_KIND_BINARY else self._anchored_code()
             c64, hist = refine_field(self._lib, self._geom, self._op, self._cur, code, self._err,
@@ -560,7 +564,9 @@ def refine_field(lib, g: TfGeom, op: TfOperator, cur: torch.Tensor, code: torch.
     """FP64 defect correction of the float32 field `cur` (updated in place with the rounding of
     the result); returns the float64 field and the max-over-volumes relative residual history.
     omega: over-relaxation of the correction sweeps (default: the solve's own). solve_e(e, r):
-    another inner solve of A e = r (float32 buffers; may overwrite r) instead of the sweeps."""
+    another inner solve of A e = r (float32 buffers; may overwrite r) instead of the sweeps; it
+    returns False when it made no progress, and the sweeps then take over (that correction is
+    dropped and the residual formed again)."""
     gp = C.byref(g)
     op0 = TfOperator.from_buffer_copy(op)
     op0.ghost_lo = op0.ghost_hi = 0.0
@@ -583,8 +589,10 @@ def refine_field(lib, g: TfGeom, op: TfOperator, cur: torch.Tensor, code: torch.
         if rel < tol or outer == max_outer:
             break
         if solve_e is not None:
-            solve_e(ea, rhs)
-            check(lib.tf_axpy_f64(gp, _ptr(c64), _ptr(ea), stream), "tf_axpy_f64")
+            if solve_e(ea, rhs):
+                check(lib.tf_axpy_f64(gp, _ptr(c64), _ptr(ea), stream), "tf_axpy_f64")
+            else:
+                solve_e = None
             continue
         ea.zero_()
         in_b = C.c_int(0)

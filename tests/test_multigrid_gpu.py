@@ -272,3 +272,26 @@ def test_kappa_with_zeros_anchored_system_matches_fp64_oracle(periodic):
     np.testing.assert_allclose(g, gref, rtol=1e-6, atol=1e-8 * np.abs(gref).max())
     # the field has conductive voxels outside the anchored system (the oracle leaves them at 0)
     assert np.any((kap > 0) & (field == 0))
+
+
+def test_multigrid_without_progress_falls_back_to_sor(monkeypatch):
+    """A multigrid inner solve that makes no progress (planted on the host) is dropped and the
+    SOR sweeps finish the FP64 correction, for KappaSolver and for the drop-in solvers."""
+    from cases import random_binary
+
+    from taufactor_gb300.multigrid import KappaMultigrid
+
+    def no_progress(self, x, r, rtol=1e-5, max_iter=200):
+        x.zero_()
+        return 0, np.ones(self.batch)
+
+    monkeypatch.setattr(KappaMultigrid, "solve", no_progress)
+    s = tg.KappaSolver(_kappa((1, 14, 12, 16), 62))
+    s.solve(conv_crit=1e-3, refine={"tol": 1e-11})
+    assert s.inner_fallback and s.residual_history[-1] < 1e-11
+    img = random_binary((2, 24, 20, 28), 41, 0.65)
+    t = tg.Solver(img)
+    t.solve(verbose=False, conv_crit=1e-3, refine={"tol": 1e-11, "max_outer": 20})
+    assert t.inner_fallback and t.residual_history[-1] < 1e-11
+    d64, _, _ = d_eff_fp64(OracleSolve(img, kind="binary"), rtol=1e-11)
+    np.testing.assert_allclose(t.D_eff, d64, rtol=1e-8, atol=1e-14)
