@@ -51,17 +51,21 @@ class KappaMultigrid:
     solver      a KappaSolver (its geometry, periodicity and packed faces)
     smooth      red/black Gauss-Seidel pairs before and after each coarse correction
     scale       coarse face factor along a halved normal axis (1/2: re-discretisation)
+    omega       over-relaxation of the smoothing half-sweeps (any value in (0, 2) keeps the
+                palindromic V-cycle symmetric)
     """
 
-    def __init__(self, solver, smooth: int = 2, scale: float = 0.5):
+    def __init__(self, solver, smooth: int = 2, scale: float = 0.5, omega: float = 1.0):
         if smooth < 1:
             raise ValueError("smooth must be >= 1")
+        if not 0.0 < omega < 2.0:
+            raise ValueError("omega must lie in (0, 2)")
         self._lib = lib = _capi.load()
         self.device = solver.device
         self.smooth = int(smooth)
         self.periodic = int(solver._op.periodic)
         op = self._op = TfOperator.from_buffer_copy(solver._op)
-        op.omega = 1.0
+        op.omega = float(np.float32(omega))
         op.ghost_lo = op.ghost_hi = 0.0
         B = solver.batch_size
         self.batch = B
