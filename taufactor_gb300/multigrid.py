@@ -9,7 +9,9 @@ once, so the inner solve costs a few dozen V-cycles at any size.
 
 Levels: the solver's own geometry and packed float32 faces, then coarse levels that halve every
 axis of extent >= 4 (tf_mg_coarsen: aggregates of 2 cells per halved axis, faces summed over the
-coarse interface and scaled by 1/2 along a halved normal axis) until every extent is below 4.
+coarse interface and scaled by 1/2 along a halved normal axis) until no extent can be halved; a
+periodic axis is halved only while its half stays even (an odd periodic extent couples cells of
+one colour across the wrap).
 Smoother: tf_kappa_advance_faces with omega 1 (red-black Gauss-Seidel), `smooth` red/black pairs
 before the coarse correction and the same number in the reverse colour order after it, so the
 V-cycle is a symmetric positive-definite preconditioner; the coarsest level takes an odd number
@@ -75,8 +77,13 @@ class KappaMultigrid:
         with torch.cuda.device(self.device):
             st = torch.cuda.current_stream(self.device).cuda_stream
             self.levels = [_Level(g0, dims, solver._fx, solver._fy, solver._fz, solver._dv, None, None)]
-            while max(dims) >= 4 and len(self.levels) < 40:
-                cd = tuple((d + 1) // 2 if d >= 4 else d for d in dims)
+            per = (False, bool(self.periodic & 1), bool(self.periodic & 2))
+            while len(self.levels) < 40:
+                # halve extents >= 4; a periodic extent only while the half stays even, so every
+                # periodic level keeps a proper red/black colouring across the wrap
+                cd = tuple((d + 1) // 2 if d >= 4 and (not p or d % 4 == 0) else d for d, p in zip(dims, per))
+                if cd == dims:
+                    break
                 g = TfGeom()
                 check(lib.tf_geometry(B, cd[0], cd[1], cd[2], self.periodic, C.byref(g)), "tf_geometry")
                 plane = g.field_elems // (B * cd[0])

@@ -295,3 +295,23 @@ def test_multigrid_without_progress_falls_back_to_sor(monkeypatch):
     assert t.inner_fallback and t.residual_history[-1] < 1e-11
     d64, _, _ = d_eff_fp64(OracleSolve(img, kind="binary"), rtol=1e-11)
     np.testing.assert_allclose(t.D_eff, d64, rtol=1e-8, atol=1e-14)
+
+
+@pytest.mark.parametrize("shape,periodic", [((2, 40, 3, 70), False), ((1, 3, 3, 3), False), ((1, 6, 40, 4), True),
+                                            ((3, 33, 17, 9), False)])
+def test_multigrid_on_thin_tiny_and_batched_shapes(shape, periodic):
+    """Semi-coarsening (extents below 4 kept), a volume with a single level, a periodic slab and
+    a batch of three: the multigrid-corrected D_eff matches the FP64 oracle to 1e-9."""
+    kap = _blurred_kappa(shape, 106, sigma=1.0)
+    s = tg.KappaSolver(kap, periodic=periodic)
+    s.solve(method="mg", refine={"tol": 1e-12})
+    assert s.converged, s.residual_history
+    levels = s.multigrid().levels
+    assert all(min(L.dims) >= 1 for L in levels)
+    if periodic:  # periodic extents stay even below the finest level
+        assert all(L.dims[1] % 2 == 0 and L.dims[2] % 2 == 0 for L in levels[1:])
+    else:
+        assert max(levels[-1].dims) < 4
+    d64, _, _ = d_eff_fp64(OracleSolve(kap, kind="periodic_kappa" if periodic else "kappa"), rtol=1e-12,
+                           coefficients="f64")
+    np.testing.assert_allclose(s.D_eff, d64, rtol=1e-9)
