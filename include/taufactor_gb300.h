@@ -343,15 +343,34 @@ int tf_anchored_phase(int batch, int nx, int ny, int nz, int periodic, const uin
  * values the sweeps use; taufactor.py:586-603 with a per-voxel diffusivity): fx_dev holds
  * batch * (nx + 1) planes of field_elems / (batch * nx) floats each (plane x + 1 = the face
  * between x and x + 1, planes 0 and nx the Dirichlet faces of planes 0 and nx - 1), fy_dev,
- * fz_dev and div_dev field_elems floats each (the +y and +z faces of every cell and the factor). */
+ * fz_dev and div_dev field_elems floats each (the +y and +z faces of every cell and the factor;
+ * the factor also on periodic ghost positions, those of the TF_PERIODIC_* bits of `periodic`). */
 int tf_kappa_faces(const tf_geom* g, const float* kappa_split_dev, float* fx_dev, float* fy_dev, float* fz_dev,
-                   float* div_dev, void* stream);
+                   float* div_dev, int periodic, void* stream);
 
 /* tf_kappa_advance from the packed faces: the same half-sweeps bit for bit, one division per
  * voxel instead of six, float4 groups (every pointer 16-byte aligned). */
 int tf_kappa_advance_faces(const tf_geom* g, const tf_operator* op, float* field_dev, const float* fx_dev,
                            const float* fy_dev, const float* fz_dev, const float* div_dev, const float* rhs_dev,
                            int first_colour, int n_half, void* stream);
+
+/* tf_kappa_advance_faces fused: K <= op->k_max (0 = 4) half-sweeps per register-streaming launch
+ * (the TMA wavefront of tf_advance; faces and factor read per group from the packed arrays), the
+ * same half-sweeps bit for bit. field_a_dev -> field_b_dev -> ... like tf_advance: *result_in_b
+ * says which buffer holds the result. Shapes the tiled kernel cannot keep periodic ghost bands
+ * for (g->tiled = 0) run tf_kappa_advance_faces in place on field_a_dev. The faces must come from
+ * tf_kappa_faces with the operator's periodic bits (the factor on periodic ghost positions), and
+ * a periodic rhs_dev must carry its ghost copies (tf_refresh_ghosts): a fused launch updates the
+ * ghost rows of its tiles like the cells they mirror. err_dev: TF_ERR_TIMEOUT if a bounded wait
+ * ran out. Every pointer 16-byte aligned. */
+int tf_kappa_advance_fused(const tf_geom* g, const tf_operator* op, float* field_a_dev, float* field_b_dev,
+                           const float* fx_dev, const float* fy_dev, const float* fz_dev, const float* div_dev,
+                           const float* rhs_dev, int first_colour, int n_half, int32_t* err_dev, int* result_in_b,
+                           void* stream);
+
+/* Periodic ghost copies of a float field in the split layout, rebuilt from the interior for the
+ * TF_PERIODIC_* bits of `periodic` (taufactor.py:501-505); nothing for 0. */
+int tf_refresh_ghosts(const tf_geom* g, int periodic, float* field_dev, void* stream);
 
 /* Coefficients of the float64 steps below (coeff_f64): 0 = the sweeps' own float32 faces and
  * float32 diagonal (the reference's discrete operator, taufactor.py:577-603); 1 = float64 faces

@@ -31,7 +31,8 @@ EXPORTS = (
     "tf_batch_advance_tile", "tf_batch_advance_rhs_tile", "tf_label_stats", "tf_anchored_phase",
     "tf_kappa_stats", "tf_mg_coarsen", "tf_mg_restrict", "tf_mg_prolong", "tf_mg_apply", "tf_mg_dot",
     "tf_pcg_update_xr", "tf_pcg_update_p", "tf_kappa_faces_f64", "tf_kappa_residual_faces_f64",
-    "tf_kappa_layer_sums_faces_f64", "tf_kappa_gradient_faces_f64",
+    "tf_kappa_layer_sums_faces_f64", "tf_kappa_gradient_faces_f64", "tf_kappa_advance_fused",
+    "tf_refresh_ghosts",
 )
 TF_IMP_TABLE = 56
 TF_BATCH_ACTIVE, TF_BATCH_CONVERGED, TF_BATCH_NEEDS_HOST = 0, 1, 2
@@ -118,7 +119,7 @@ def load():
         "tf_batch_converge_static": (i32, [vp, vp, i32, i32, i64, i64, TfBatchState, C.c_double, i32, i32, vp]),
         "tf_kappa_pack": (i32, [G, O, vp, vp, vp, vp, vp]),
         "tf_kappa_advance": (i32, [G, O, vp, vp, vp, i32, i32, vp]),
-        "tf_kappa_faces": (i32, [G, vp, vp, vp, vp, vp, vp]),
+        "tf_kappa_faces": (i32, [G, vp, vp, vp, vp, vp, i32, vp]),
         "tf_spans_x": (i32, [i32, i32, i32, i32, vp, vp, vp, vp, vp, vp]),
         "tf_impedance_pack": (i32, [i32, i32, i32, i32, vp, vp, vp, vp]),
         "tf_impedance_fill": (i32, [i32, i32, i32, i32, vp, vp, C.c_double, vp, vp]),
@@ -138,6 +139,8 @@ def load():
         "tf_pcg_update_xr": (i32, [G, vp, vp, vp, vp, vp, vp, vp]),
         "tf_pcg_update_p": (i32, [G, vp, vp, vp, vp, vp]),
         "tf_kappa_faces_f64": (i32, [G, vp, vp, vp, vp, vp, vp]),
+        "tf_kappa_advance_fused": (i32, [G, O, vp, vp, vp, vp, vp, vp, vp, i32, i32, vp, C.POINTER(C.c_int), vp]),
+        "tf_refresh_ghosts": (i32, [G, i32, vp, vp]),
         "tf_kappa_residual_faces_f64": (i32, [G, O, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),
         "tf_kappa_layer_sums_faces_f64": (i32, [G, vp, vp, vp, vp, vp]),
         "tf_kappa_gradient_faces_f64": (i32, [G, O, vp, vp, vp, vp, vp, vp, vp, C.c_double, C.c_double, C.c_double,

@@ -153,9 +153,10 @@ __global__ void __launch_bounds__(256) k_kappa_sweep(float* __restrict__ c, cons
 //      and x' = NX hold the Dirichlet faces hface(k, k) of planes 0 and NX - 1
 //   fy [b][x][Y][...]: the face between padded rows Y and Y + 1 (0 past the last padded row)
 //   fz [b][x][Y][q][jp]: the face between cell z = 2 (jp - HJ) + q and z + 1 (0 past the row)
-//   dv [b][x][Y][q][jp]: the factor of kappa_faces for interior cells, inf elsewhere
+//   dv [b][x][Y][q][jp]: the factor of kappa_faces for interior cells and periodic ghost
+//      positions (the wrapped cell's), inf elsewhere
 __global__ void k_kappa_face_pack(const float* __restrict__ kp, float* __restrict__ fx, float* __restrict__ fy,
-                                  float* __restrict__ fz, float* __restrict__ dv, const Geo g) {
+                                  float* __restrict__ fz, float* __restrict__ dv, const Geo g, int periodic) {
     const int pos = blockIdx.x * blockDim.x + threadIdx.x;  // q * ZH + jp
     if (pos >= 2 * g.ZH) return;
     const int Y = blockIdx.y;
@@ -171,11 +172,23 @@ __global__ void k_kappa_face_pack(const float* __restrict__ kp, float* __restric
     const long long fxo = ((long long)b * (g.NX + 1) + x) * g.plane_f + (long long)Y * g.row_f + pos;
     fx[fxo + g.plane_f] = x + 1 < g.NX ? hface(kc, kp[o + g.plane_f]) : hface(kc, kc);
     if (x == 0) fx[fxo] = hface(kc, kc);
-    const int y = Y - HY, z = 2 * (jp - HJ) + q;
+    // the factor of interior cells, and on periodic ghost positions that of the wrapped cell (a
+    // fused sweep updates the ghost copies of its tile's halo like the cells they mirror)
+    int y = Y - HY, z = 2 * (jp - HJ) + q;
+    bool ok = true;
+    if (y < 0 || y >= g.NY) {
+        ok = ok && (periodic & TF_PERIODIC_Y);
+        y = wrap(y, g.NY);
+    }
+    if (z < 0 || z >= g.NZ) {
+        ok = ok && (periodic & TF_PERIODIC_Z);
+        z = wrap(z, g.NZ);
+    }
     float d = __int_as_float(0x7f800000);
-    if (y >= 0 && y < g.NY && jp >= HJ && z < g.NZ) {
+    if (ok) {
         const KView v{g};
-        d = kappa_faces(kp + (long long)b * g.vol_f, v, x, y, z, kc).div;
+        const float* kb = kp + (long long)b * g.vol_f;
+        d = kappa_faces(kb, v, x, y, z, kb[v.off(x, y, z)]).div;
     }
     dv[o] = d;
 }
@@ -736,11 +749,12 @@ int tf_kappa_advance(const tf_geom* g, const tf_operator* op, float* field_dev, 
 }
 
 int tf_kappa_faces(const tf_geom* g, const float* kappa_split_dev, float* fx_dev, float* fy_dev, float* fz_dev,
-                   float* div_dev, void* stream) {
+                   float* div_dev, int periodic, void* stream) {
     if (!g || !kappa_split_dev || !fx_dev || !fy_dev || !fz_dev || !div_dev) return TF_ERR_ARG;
     const Geo geo = make_geo(*g);
     dim3 grid((2 * g->zh + 127) / 128, g->yp, g->batch * g->nx);
-    k_kappa_face_pack<<<grid, 128, 0, (cudaStream_t)stream>>>(kappa_split_dev, fx_dev, fy_dev, fz_dev, div_dev, geo);
+    k_kappa_face_pack<<<grid, 128, 0, (cudaStream_t)stream>>>(kappa_split_dev, fx_dev, fy_dev, fz_dev, div_dev, geo,
+                                                               periodic);
     note_launch();
     return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
 }

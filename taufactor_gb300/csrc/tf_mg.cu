@@ -72,7 +72,8 @@ __device__ __forceinline__ float residual_at(const Geo& g, int b, int x, int y, 
 }  // namespace
 
 // One thread per padded position of the coarse level; periodic ghost positions hold the faces
-// of the wrapped cell, closed ghost positions 0 (factor inf), as k_kappa_face_pack writes them.
+// and factor of the wrapped cell, closed ghost positions 0 (factor inf), as k_kappa_face_pack
+// writes them.
 __global__ void k_mg_coarsen(const float* __restrict__ fx, const float* __restrict__ fy, const float* __restrict__ fz,
                              const Geo f, float* __restrict__ cfx, float* __restrict__ cfy, float* __restrict__ cfz,
                              float* __restrict__ cdv, const Geo c, const Shift sh, int periodic, float scale) {
@@ -84,7 +85,6 @@ __global__ void k_mg_coarsen(const float* __restrict__ fx, const float* __restri
     const int q = pos >= c.ZH ? 1 : 0;
     const int jp = pos - q * c.ZH;
     int yc = Y - HY, zc = 2 * (jp - HJ) + q;
-    const bool interior = yc >= 0 && yc < c.NY && zc >= 0 && zc < c.NZ;
     bool ok = true;
     if (yc < 0 || yc >= c.NY) {
         ok = ok && (periodic & TF_PERIODIC_Y);
@@ -131,8 +131,9 @@ __global__ void k_mg_coarsen(const float* __restrict__ fx, const float* __restri
     cfz[o] = zp;
     cfx[ox + c.plane_f] = xp;
     if (xc == 0) cfx[ox] = xm;
+    // the factor on interior cells and periodic ghost positions (the wrapped cell's)
     float d = kInf;
-    if (interior) {
+    {
         d = xm + xp;
         d += ym;
         d += yp;

@@ -92,12 +92,46 @@ __device__ __forceinline__ SlotOffsets slot_offsets(int ty, int jj, int q, int W
 //   zo: the other half-row group of this plane (registers); y-neighbours and the z-edge cell of
 //   the adjacent group are read from the plane's shared-memory slot (field offsets fo, code
 //   offsets co), and the result is published there.
+__device__ __forceinline__ void prefetch_l2(const float* p) { asm volatile("prefetch.global.L2 [%0];" ::"l"(p)); }
+
+// KIND_FACES: the packed faces and factor of a thread's group at global offset `go` (the group's
+// first padded cell of half-row 0, or -1 outside the padded plane: no faces, factor inf);
+// `ym_ok`: the row above exists in the padded plane; `zm_ok`: the cell before the group does.
+struct GroupFaces {
+    float4 xp, xm, yp, ym, zp, zm, d;
+};
+__device__ __forceinline__ GroupFaces load_faces(const SweepArgs& a, long long go, int b, int q, bool ym_ok,
+                                                 bool zm_ok) {
+    GroupFaces f;
+    const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (go < 0) {
+        f.xp = f.xm = f.yp = f.ym = f.zp = f.zm = zero4;
+        const float inf = __int_as_float(0x7f800000);
+        f.d = make_float4(inf, inf, inf, inf);
+        return f;
+    }
+    const Geo& g = a.g;
+    const long long o = go + q * g.ZH, oo = go + (q ^ 1) * g.ZH;  // this half-row, the other one
+    const long long ox = o + (long long)b * g.plane_f;           // fx plane p: the face to p - 1
+    f.xm = __ldg(reinterpret_cast<const float4*>(a.fx + ox));
+    f.xp = __ldg(reinterpret_cast<const float4*>(a.fx + ox + g.plane_f));
+    f.yp = __ldg(reinterpret_cast<const float4*>(a.fy + o));
+    f.ym = ym_ok ? __ldg(reinterpret_cast<const float4*>(a.fy + o - g.row_f)) : zero4;
+    f.zp = __ldg(reinterpret_cast<const float4*>(a.fz + o));
+    const float4 fo = __ldg(reinterpret_cast<const float4*>(a.fz + oo));
+    // the face between z - 1 and z, stored at cell z - 1 (other half-row, j - 1 for q = 0)
+    f.zm = q ? fo : make_float4(zm_ok ? __ldg(a.fz + oo - 1) : 0.0f, fo.x, fo.y, fo.z);
+    f.d = __ldg(reinterpret_cast<const float4*>(a.dv + o));
+    return f;
+}
+
 template <int KIND, bool RHS>
 __device__ __forceinline__ void stage_update(float4& self, const float4& xp, const float4& xm, const float4& zo,
                                              uint32_t cc, uint32_t cxp, uint32_t cxm, uint32_t czo, float* Fp,
                                              const unsigned char* Cp, SlotOffsets fo, SlotOffsets co, int q, int WJ,
                                              int WJC, bool at_lo, bool at_hi, const SweepArgs& a, const float* lut,
-                                             const float4* tab, const float* rhs_row) {
+                                             const float4* tab, const float* rhs_row, long long go = -1, int b = 0,
+                                             bool ym_ok = false, bool zm_ok = false) {
     // right-hand side of a correction solve (A e = r): the thread's 4 cells, read-only path
     float4 rv = make_float4(0.f, 0.f, 0.f, 0.f);
     if (RHS && rhs_row) rv = __ldg(reinterpret_cast<const float4*>(rhs_row + q * a.g.ZH));
@@ -106,6 +140,12 @@ __device__ __forceinline__ void stage_update(float4& self, const float4& xp, con
     const float e = Fp[fo.e];
     float4 zp, zm;
     z_neighbours(q, zo, e, zp, zm);
+    if (KIND == KIND_FACES) {
+        const GroupFaces f = load_faces(a, go, b, q, ym_ok, zm_ok);
+        self = update4_faces<RHS>(self, xp, xm, yp, ym, zp, zm, f.xp, f.xm, f.yp, f.ym, f.zp, f.zm, f.d, a.omega, rv);
+        st4(Fp + fo.me, self);
+        return;
+    }
     uint32_t cyp = 0, cym = 0, czp = 0, czm = 0;
     if (KIND == TF_KIND_MULTIPHASE) {
         cyp = ld_u32(Cp + co.me + 2 * WJC);
@@ -178,9 +218,9 @@ __device__ __forceinline__ void stream_tile(const CUtensorMap* tmf, const CUtens
     const int xe = x1 + K < NX ? x1 + K : NX;
     auto issue = [&](int x) {
         const int s = (int)((unsigned)(x - xs) % NS);
-        mbar_arrive_expect_tx(&bar[s], S::FBYTES + S::CBYTES);
+        mbar_arrive_expect_tx(&bar[s], S::FBYTES + (KIND == KIND_FACES ? 0 : S::CBYTES));
         tma_load_3d(F0 + s * (S::SLOT / 4), tmf, &bar[s], j0, row0, b * NX + x);
-        tma_load_3d(C0 + s * S::SLOT, tmc, &bar[s], j0, row0, b * NX + x);
+        if (KIND != KIND_FACES) tma_load_3d(C0 + s * S::SLOT, tmc, &bar[s], j0, row0, b * NX + x);
     };
     if (tid == 0)
         for (int x = xs; x < xs + D && x < xe; ++x) issue(x);
@@ -212,6 +252,20 @@ __device__ __forceinline__ void stream_tile(const CUtensorMap* tmf, const CUtens
             const int t = t0 + i;
             if (t < total) {
                 if (tid == 0 && t + D < xe) issue(t + D);
+                if (KIND == KIND_FACES && t < NX && y >= -HY && y < g.NY + HY && j0 + jj + 4 <= g.ZH) {
+                    // the faces of plane t, first used one step later: into L2 now, so that the
+                    // stages' loads do not wait on DRAM in the middle of their dependent chain
+                    const long long go = (long long)b * g.vol_f + (long long)t * g.plane_f +
+                                         (long long)(y + HY) * g.row_f + j0 + jj;
+#pragma unroll
+                    for (int q = 0; q < 2; ++q) {
+                        const long long o = go + q * g.ZH;
+                        prefetch_l2(a.fx + o + (long long)b * g.plane_f);
+                        prefetch_l2(a.fy + o);
+                        prefetch_l2(a.fz + o);
+                        prefetch_l2(a.dv + o);
+                    }
+                }
                 if (t < xe) {
                     const int slot = (int)((unsigned)(t - xs) % NS);
                     if (!mbar_wait_bounded(&bar[slot], ((unsigned)(t - xs) / NS) & 1)) *s_fail = 1;
@@ -219,8 +273,9 @@ __device__ __forceinline__ void stream_tile(const CUtensorMap* tmf, const CUtens
                     const unsigned char* Cs = C0 + slot * S::SLOT;
                     const float4 e4 = ld4(Fs + (2 * ty) * WJ + jj);
                     const float4 o4 = ld4(Fs + (2 * ty + 1) * WJ + jj);
-                    const uint32_t ce = ld_u32(Cs + (2 * ty) * WJC + jj);
-                    const uint32_t co = ld_u32(Cs + (2 * ty + 1) * WJC + jj);
+                    // (KIND_FACES stages no codes)
+                    const uint32_t ce = KIND == KIND_FACES ? 0u : ld_u32(Cs + (2 * ty) * WJC + jj);
+                    const uint32_t co = KIND == KIND_FACES ? 0u : ld_u32(Cs + (2 * ty + 1) * WJC + jj);
                     const bool even0 = ((t + y + c0) & 1) == 0;  // even-z cells have relative colour 0
                     V0[i] = even0 ? e4 : o4;
                     V1[i] = even0 ? o4 : e4;
@@ -249,18 +304,27 @@ __device__ __forceinline__ void stream_tile(const CUtensorMap* tmf, const CUtens
                         const bool at_lo = p == 0, at_hi = p == NX - 1;
                         // global address of this thread's group in the right-hand side (padded
                         // coordinates; rows beyond the ghost bands and groups past the row read 0)
+                        const bool in_plane = y >= -HY && y < g.NY + HY && j0 + jj + 4 <= g.ZH;
                         const float* rhs_row = nullptr;
-                        if (RHS && y >= -HY && y < g.NY + HY && j0 + jj + 4 <= g.ZH)
+                        if (RHS && in_plane)
                             rhs_row = a.rhs + (long long)b * g.vol_f + (long long)p * g.plane_f +
                                       (long long)(y + HY) * g.row_f + j0 + jj;
+                        // KIND_FACES: global offset of the group's faces (half-row 0), -1 if none
+                        const long long go = KIND == KIND_FACES && in_plane
+                                                 ? (long long)b * g.vol_f + (long long)p * g.plane_f +
+                                                       (long long)(y + HY) * g.row_f + j0 + jj
+                                                 : -1LL;
+                        const bool ym_ok = y + HY > 0, zm_ok = j0 + jj > 0;
                         if (((s - 1) & 1) == 0) {
                             const uint32_t cxp = at_hi ? K0[ip] : K1[ipn], cxm = at_lo ? K0[ip] : K1[ipp];
                             stage_update<KIND, RHS>(V0[ip], V1[ipn], V1[ipp], V1[ip], K0[ip], cxp, cxm, K1[ip], Fp,
-                                                    Cp, fo, co, qs, WJ, WJC, at_lo, at_hi, a, lut, tab, rhs_row);
+                                                    Cp, fo, co, qs, WJ, WJC, at_lo, at_hi, a, lut, tab, rhs_row, go,
+                                                    b, ym_ok, zm_ok);
                         } else {
                             const uint32_t cxp = at_hi ? K1[ip] : K0[ipn], cxm = at_lo ? K1[ip] : K0[ipp];
                             stage_update<KIND, RHS>(V1[ip], V0[ipn], V0[ipp], V0[ip], K1[ip], cxp, cxm, K0[ip], Fp,
-                                                    Cp, fo, co, qs, WJ, WJC, at_lo, at_hi, a, lut, tab, rhs_row);
+                                                    Cp, fo, co, qs, WJ, WJC, at_lo, at_hi, a, lut, tab, rhs_row, go,
+                                                    b, ym_ok, zm_ok);
                         }
                     }
                 }
@@ -372,20 +436,32 @@ static int prepare_kernel(int threads, int smem) {
 
 template <int KIND, int TY, int TZ, int K, bool RHS>
 static int launch_stream(const tf_geom& gg, const tf_operator& op, const float* in, float* out, const uint8_t* code,
-                         const float* rhs, int first_colour, int32_t* err, cudaStream_t st) {
+                         const float* rhs, int first_colour, int32_t* err, cudaStream_t st,
+                         const float* const* faces = nullptr) {
     using S = StreamShape<TY, TZ, K>;
     CUtensorMap tmf, tmc;
     int rc = encode_map_3d(&tmf, in, 4, gg.zh, 2 * gg.yp, (long long)gg.batch * gg.nx, (long long)gg.zh * 4,
                            (long long)gg.zh * 4 * 2 * gg.yp, S::WJ, 2 * S::ROWS);
     if (rc) return rc;
-    rc = encode_map_3d(&tmc, code, 1, gg.zhc, 2 * gg.yp, (long long)gg.batch * gg.nx, gg.zhc,
-                       (long long)gg.zhc * 2 * gg.yp, S::WJC, 2 * S::ROWS);
-    if (rc) return rc;
+    if (KIND == KIND_FACES) {
+        if (!faces) return TF_ERR_ARG;
+        tmc = tmf;  // no codes: the map is passed but never read
+    } else {
+        rc = encode_map_3d(&tmc, code, 1, gg.zhc, 2 * gg.yp, (long long)gg.batch * gg.nx, gg.zhc,
+                           (long long)gg.zhc * 2 * gg.yp, S::WJC, 2 * S::ROWS);
+        if (rc) return rc;
+    }
     constexpr auto kern = k_stream<KIND, TY, TZ, K, RHS>;
     const int resident = prepare_kernel<kern>(S::NT, S::SMEM);  // CTAs of this kernel per SM
     if (resident <= 0) return TF_ERR_CUDA;
     SweepArgs a = make_args(make_geo(gg), op, out, first_colour, K, err);
     a.rhs = rhs;
+    if (faces) {
+        a.fx = faces[0];
+        a.fy = faces[1];
+        a.fz = faces[2];
+        a.dv = faces[3];
+    }
     const long long columns = (long long)((gg.nz + TZ - 1) / TZ) * ((gg.ny + TY - 1) / TY) * gg.batch;
     a.x_chunks = x_chunks_for(columns, gg.nx, K, resident * sm_count());
     if ((long long)gg.batch * a.x_chunks > 65535) a.x_chunks = 1;  // grid z limit

@@ -138,6 +138,7 @@ SweepArgs make_args(const Geo& g, const tf_operator& op, float* out, int first_c
     a.periodic = op.periodic;
     a.x_chunks = 1;
     a.rhs = nullptr;
+    a.fx = a.fy = a.fz = a.dv = nullptr;
     return a;
 }
 

@@ -13,7 +13,14 @@ struct SweepArgs {
     int x_chunks;      // x-chunks per tile column of the fused sweep (grid z = batch * x_chunks)
     int32_t* err;
     const float* rhs;  // right-hand side of a correction solve (split layout), or null
+    // KIND_FACES: the packed per-voxel faces and factor (k_kappa_face_pack's layout), else null
+    const float *fx, *fy, *fz, *dv;
 };
+
+// Internal operator kind of the fused sweep: per-voxel faces and factor read from the packed
+// arrays of SweepArgs instead of derived from codes (the per-voxel conductivity operator, and
+// MultiPhaseSolver's with kappa = D[label]).
+constexpr int KIND_FACES = 16;
 
 SweepArgs make_args(const Geo& g, const tf_operator& op, float* out, int first_colour, int n_half, int32_t* err);
 
@@ -224,6 +231,27 @@ __device__ __forceinline__ float4 update4(float4 c, const float4& xp, const floa
             quot = quotient(sum, div);
         }
         set_comp(c, i, sor_finish(ci, quot, omega));
+    }
+    return c;
+}
+
+// One float4 group from packed faces: k_kappa_sweep4's arithmetic (taufactor.py:607-612, products
+// then the left-to-right sum, over the packed factor; inf where frozen), so the same bits.
+template <bool RHS>
+__device__ __forceinline__ float4 update4_faces(float4 c, const float4& xp, const float4& xm, const float4& yp,
+                                                const float4& ym, const float4& zp, const float4& zm,
+                                                const float4& fxp, const float4& fxm, const float4& fyp,
+                                                const float4& fym, const float4& fzp, const float4& fzm,
+                                                const float4& d, float omega, const float4& rv) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        float s = __fadd_rn(__fmul_rn(comp(xp, i), comp(fxp, i)), __fmul_rn(comp(xm, i), comp(fxm, i)));
+        s = __fadd_rn(s, __fmul_rn(comp(yp, i), comp(fyp, i)));
+        s = __fadd_rn(s, __fmul_rn(comp(ym, i), comp(fym, i)));
+        s = __fadd_rn(s, __fmul_rn(comp(zp, i), comp(fzp, i)));
+        s = __fadd_rn(s, __fmul_rn(comp(zm, i), comp(fzm, i)));
+        if (RHS) s = __fadd_rn(s, comp(rv, i));
+        set_comp(c, i, sor_finish(comp(c, i), quotient(s, comp(d, i)), omega));
     }
     return c;
 }

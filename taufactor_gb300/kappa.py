@@ -128,7 +128,7 @@ class KappaSolver:
             self._fz = torch.empty(g.field_elems, **f32)
             self._dv = torch.empty(g.field_elems, **f32)
             check(lib.tf_kappa_faces(C.byref(g), _ptr(self._ks), _ptr(self._fx), _ptr(self._fy), _ptr(self._fz),
-                                     _ptr(self._dv), st), "tf_kappa_faces")
+                                     _ptr(self._dv), pflag, st), "tf_kappa_faces")
             self._flux = torch.empty((self.batch_size, self.Nx - 1), dtype=torch.float64, device=self.device)
             self._csum = torch.empty((self.batch_size, self.Nx), dtype=torch.float64, device=self.device)
         self._c64 = None
@@ -145,6 +145,9 @@ class KappaSolver:
 
     # ---------------------------------------------------------------- forward
     def _advance(self, n: int, field: torch.Tensor, rhs=None, op=None, first_colour=None):
+        """n half-sweeps of `field` in place from the packed faces (tf_kappa_advance_faces: one
+        half-sweep per launch, HBM-bound; the fused form tf_kappa_advance_fused computes the same
+        bits and measured slower on this operator)."""
         check(self._lib.tf_kappa_advance_faces(C.byref(self._geom), C.byref(op or self._op), _ptr(field),
                                                _ptr(self._fx), _ptr(self._fy), _ptr(self._fz), _ptr(self._dv),
                                                _ptr(rhs) if rhs is not None else None,
@@ -287,7 +290,7 @@ class KappaSolver:
                 fx = torch.empty(self.batch_size * (self.Nx + 1) * plane, **f32)
                 fy, fz, dv = (torch.empty(g.field_elems, **f32) for _ in range(3))
                 check(self._lib.tf_kappa_faces(C.byref(g), _ptr(self._kappa64()), _ptr(fx), _ptr(fy), _ptr(fz),
-                                               _ptr(dv), self._stream()), "tf_kappa_faces")
+                                               _ptr(dv), int(self._op.periodic), self._stream()), "tf_kappa_faces")
                 view = SimpleNamespace(device=self.device, _op=self._op, batch_size=self.batch_size, Nx=self.Nx,
                                        Ny=self.Ny, Nz=self.Nz, _geom=g, _fx=fx, _fy=fy, _fz=fz, _dv=dv)
             self._mg = KappaMultigrid(view)

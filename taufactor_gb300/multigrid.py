@@ -99,7 +99,7 @@ class KappaMultigrid:
             # odd length: a palindrome of half-sweeps from zero, so the coarsest solve is symmetric
             self.coarse_half_sweeps = 2 * sum(self.levels[-1].dims) + 1
             n = g0.field_elems
-            self._z = torch.zeros(n, **f32)
+            self.levels[0].e = torch.zeros(n, **f32)  # z = M^-1 r of the conjugate gradients
             self._p = torch.zeros(n, **f32)
             self._q = torch.zeros(n, **f32)
             self._part = torch.empty(2 * B * solver.Nx * solver.Ny, dtype=torch.float64, device=self.device)
@@ -109,27 +109,31 @@ class KappaMultigrid:
     def _st(self):
         return torch.cuda.current_stream(self.device).cuda_stream
 
-    def _smooth(self, L, e, b, first_colour, n):
-        check(self._lib.tf_kappa_advance_faces(C.byref(L.geom), C.byref(self._op), _ptr(e), _ptr(L.fx), _ptr(L.fy),
-                                               _ptr(L.fz), _ptr(L.dv), _ptr(b), first_colour, n, self._st()),
-              "tf_kappa_advance_faces")
+    def _smooth(self, L, b, first_colour, n):
+        """n half-sweeps of L.e in place with right-hand side b (tf_kappa_advance_faces; the fused
+        form computes the same bits and measured slower on this operator)."""
+        check(self._lib.tf_kappa_advance_faces(C.byref(L.geom), C.byref(self._op), _ptr(L.e), _ptr(L.fx),
+                                               _ptr(L.fy), _ptr(L.fz), _ptr(L.dv), _ptr(b), first_colour, n,
+                                               self._st()), "tf_kappa_advance_faces")
 
-    def vcycle(self, level: int, b: torch.Tensor, e: torch.Tensor) -> None:
-        """e = (V-cycle from zero) applied to b on `level`."""
+    def vcycle(self, level: int, b: torch.Tensor) -> torch.Tensor:
+        """The V-cycle from zero applied to b on `level`; returns the buffer holding the result
+        (the level's e)."""
         L = self.levels[level]
-        e.zero_()
+        L.e.zero_()
         if level == len(self.levels) - 1:
-            self._smooth(L, e, b, 0, self.coarse_half_sweeps)
-            return
-        self._smooth(L, e, b, 0, 2 * self.smooth)
+            self._smooth(L, b, 0, self.coarse_half_sweeps)
+            return L.e
+        self._smooth(L, b, 0, 2 * self.smooth)
         Cl = self.levels[level + 1]
         lib, st = self._lib, self._st()
-        check(lib.tf_mg_restrict(C.byref(L.geom), _ptr(e), _ptr(b), _ptr(L.fx), _ptr(L.fy), _ptr(L.fz), _ptr(L.dv),
+        check(lib.tf_mg_restrict(C.byref(L.geom), _ptr(L.e), _ptr(b), _ptr(L.fx), _ptr(L.fy), _ptr(L.fz), _ptr(L.dv),
                                  C.byref(Cl.geom), _ptr(Cl.b), st), "tf_mg_restrict")
-        self.vcycle(level + 1, Cl.b, Cl.e)
-        check(lib.tf_mg_prolong(C.byref(Cl.geom), _ptr(Cl.e), C.byref(L.geom), _ptr(e), self.periodic, st),
+        ec = self.vcycle(level + 1, Cl.b)
+        check(lib.tf_mg_prolong(C.byref(Cl.geom), _ptr(ec), C.byref(L.geom), _ptr(L.e), self.periodic, st),
               "tf_mg_prolong")
-        self._smooth(L, e, b, 1, 2 * self.smooth)
+        self._smooth(L, b, 1, 2 * self.smooth)
+        return L.e
 
     def _dot(self, out, a1, b1, a2=None, b2=None):
         check(self._lib.tf_mg_dot(C.byref(self.levels[0].geom), _ptr(a1), _ptr(b1), _ptr(a2), _ptr(b2),
@@ -142,12 +146,12 @@ class KappaMultigrid:
         lib, L0 = self._lib, self.levels[0]
         g = C.byref(L0.geom)
         B = self.batch
-        z, p, q = self._z, self._p, self._q
+        p, q = self._p, self._q
         rz, rz_new, rr = self._d
         with torch.cuda.device(self.device):
             st = self._st()
             x.zero_()
-            self.vcycle(0, r, z)
+            z = self.vcycle(0, r)
             p.copy_(z)
             self._dot(rz, r, z, r, r)
             rr0 = rz[B:].cpu().numpy().copy()
@@ -161,7 +165,7 @@ class KappaMultigrid:
                 self._dot(rr, p, q)  # rr[:B] = p.q
                 check(lib.tf_pcg_update_xr(g, _ptr(x), _ptr(r), _ptr(p), _ptr(q), _ptr(rz), _ptr(rr), st),
                       "tf_pcg_update_xr")
-                self.vcycle(0, r, z)
+                z = self.vcycle(0, r)
                 self._dot(rz_new, r, z, r, r)
                 rel = np.sqrt(np.maximum(rz_new[B:].cpu().numpy(), 0.0) / rr0)
                 check(lib.tf_pcg_update_p(g, _ptr(p), _ptr(z), _ptr(rz_new), _ptr(rz), st), "tf_pcg_update_p")

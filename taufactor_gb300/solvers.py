@@ -300,8 +300,8 @@ class SORSolver:
         plane = g.field_elems // (self.batch_size * self.Nx)
         fx = torch.empty(self.batch_size * (self.Nx + 1) * plane, **f32)
         fy, fz, dv = (torch.empty(g.field_elems, **f32) for _ in range(3))
-        check(self._lib.tf_kappa_faces(C.byref(g), _ptr(ks), _ptr(fx), _ptr(fy), _ptr(fz), _ptr(dv), st),
-              "tf_kappa_faces")
+        check(self._lib.tf_kappa_faces(C.byref(g), _ptr(ks), _ptr(fx), _ptr(fy), _ptr(fz), _ptr(dv), self._periodic,
+                                       st), "tf_kappa_faces")
         del ks
         view = SimpleNamespace(device=dev, _op=self._op, batch_size=self.batch_size, Nx=self.Nx, Ny=self.Ny,
                                Nz=self.Nz, _geom=g, _fx=fx, _fy=fy, _fz=fz, _dv=dv)

@@ -217,3 +217,47 @@ def test_design_loop_warm_started_steps():
     fd = (deff(kp) - deff(km)) / 2.0
     ad = float((g * ((kp.double() - km.double()) / 2.0)).sum())
     assert abs(fd - ad) / abs(fd) < 1e-6
+
+
+@pytest.mark.parametrize("k_max", [1, 3, 4])
+@pytest.mark.parametrize("periodic", [False, True])
+@pytest.mark.parametrize("shape", [(1, 9, 12, 18), (2, 37, 20, 40), (1, 40, 36, 130), (2, 150, 16, 64)])
+def test_fused_face_sweeps_equal_single_sweeps(shape, periodic, k_max):
+    """tf_kappa_advance_fused (K half-sweeps per register-streaming launch, faces read per group)
+    gives tf_kappa_advance_faces's bits: kappa with zeros, partial tiles in y and z, x-chunked
+    columns, periodic ghost bands, with and without a right-hand side, both colour starts."""
+    import ctypes as C
+
+    from taufactor_gb300._capi import TfOperator, check
+
+    rng = np.random.default_rng(sum(shape) + k_max)
+    kap = (rng.random(shape) * (rng.random(shape) > 0.2)).astype(np.float32)
+    s = tg.KappaSolver(kap, periodic=periodic)
+    lib, g, st = s._lib, s._geom, s._stream()
+    op = TfOperator.from_buffer_copy(s._op)
+    op.k_max = k_max
+    a = s._c.clone()
+    fa, fb = s._c.clone(), torch.zeros_like(s._c)
+    rhs = (0.01 * torch.randn(g.field_elems, device="cuda")).float()
+    rhs[s._ks == 0] = 0
+    check(lib.tf_refresh_ghosts(C.byref(g), s._op.periodic, rhs.data_ptr(), st), "tf_refresh_ghosts")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    faces = [s._fx.data_ptr(), s._fy.data_ptr(), s._fz.data_ptr(), s._dv.data_ptr()]
+    for n, r, c0 in ((4, None, 0), (7, rhs, 1), (5, None, 1), (8, rhs, 0)):
+        rp = r.data_ptr() if r is not None else None
+        check(lib.tf_kappa_advance_faces(C.byref(g), C.byref(op), a.data_ptr(), *faces, rp, c0, n, st),
+              "tf_kappa_advance_faces")
+        in_b = C.c_int(0)
+        check(lib.tf_kappa_advance_fused(C.byref(g), C.byref(op), fa.data_ptr(), fb.data_ptr(), *faces, rp, c0, n,
+                                         err.data_ptr(), C.byref(in_b), st), "tf_kappa_advance_fused")
+        if in_b.value:
+            fa, fb = fb, fa
+        torch.cuda.synchronize()
+        assert int(err.item()) == 0
+        m = torch.zeros(g.field_elems, dtype=torch.bool, device="cuda")
+        lay_row, lay_plane = 2 * g.zh, 2 * g.zh * g.yp
+        b_, x_, y_, z_ = np.meshgrid(np.arange(s.batch_size), np.arange(s.Nx), np.arange(s.Ny), np.arange(s.Nz),
+                                     indexing="ij")
+        idx = (b_ * s.Nx + x_) * lay_plane + (y_ + 4) * lay_row + (z_ & 1) * g.zh + 4 + (z_ >> 1)
+        m[torch.from_numpy(idx.ravel()).cuda()] = True
+        assert torch.equal(a[m].view(torch.int32), fa[m].view(torch.int32)), n
