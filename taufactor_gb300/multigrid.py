@@ -47,6 +47,20 @@ class _Level:
         self.e, self.b = e, b
 
 
+def level_dims(dims, periodic: int, max_levels: int = 40) -> list:
+    """Extents (nx, ny, nz) of every level, finest first: each coarser level halves every extent
+    >= 4 (rounding up), a periodic one (TF_PERIODIC_Y / _Z bits of `periodic`) only while the
+    half stays even, until no extent can be halved."""
+    per = (False, bool(periodic & 1), bool(periodic & 2))
+    out = [tuple(int(d) for d in dims)]
+    while len(out) < max_levels:
+        cd = tuple((d + 1) // 2 if d >= 4 and (not p or d % 4 == 0) else d for d, p in zip(out[-1], per))
+        if cd == out[-1]:
+            break
+        out.append(cd)
+    return out
+
+
 class KappaMultigrid:
     """V-cycle PCG on a KappaSolver's operator (float32 faces, homogeneous Dirichlet x faces).
 
@@ -77,13 +91,9 @@ class KappaMultigrid:
         with torch.cuda.device(self.device):
             st = torch.cuda.current_stream(self.device).cuda_stream
             self.levels = [_Level(g0, dims, solver._fx, solver._fy, solver._fz, solver._dv, None, None)]
-            per = (False, bool(self.periodic & 1), bool(self.periodic & 2))
-            while len(self.levels) < 40:
-                # halve extents >= 4; a periodic extent only while the half stays even, so every
-                # periodic level keeps a proper red/black colouring across the wrap
-                cd = tuple((d + 1) // 2 if d >= 4 and (not p or d % 4 == 0) else d for d, p in zip(dims, per))
-                if cd == dims:
-                    break
+            # a periodic extent is halved only while the half stays even, so every periodic level
+            # keeps a proper red/black colouring across the wrap
+            for cd in level_dims(dims, self.periodic)[1:]:
                 g = TfGeom()
                 check(lib.tf_geometry(B, cd[0], cd[1], cd[2], self.periodic, C.byref(g)), "tf_geometry")
                 plane = g.field_elems // (B * cd[0])
@@ -95,7 +105,6 @@ class KappaMultigrid:
                       "tf_mg_coarsen")
                 self.levels.append(_Level(g, cd, fx, fy, fz, dv, torch.zeros(g.field_elems, **f32),
                                           torch.zeros(g.field_elems, **f32)))
-                dims = cd
             # odd length: a palindrome of half-sweeps from zero, so the coarsest solve is symmetric
             self.coarse_half_sweeps = 2 * sum(self.levels[-1].dims) + 1
             n = g0.field_elems

@@ -171,3 +171,23 @@ def test_multiphase_missing_label_warning_before_device():
             pass
     assert any("assuming these phases are isolating." in str(x.message) for x in w)
     assert ds[2] == 0.0
+
+
+def test_multigrid_level_dims():
+    """The multigrid hierarchy's shapes: extents >= 4 halve (rounding up), smaller ones stay,
+    periodic extents only while the half is even; the coarsest level cannot be halved again."""
+    from taufactor_gb300.multigrid import level_dims
+
+    assert level_dims((768, 768, 768), 0) == [(768,) * 3, (384,) * 3, (192,) * 3, (96,) * 3, (48,) * 3,
+                                              (24,) * 3, (12,) * 3, (6,) * 3, (3,) * 3]
+    assert level_dims((40, 3, 70), 0) == [(40, 3, 70), (20, 3, 35), (10, 3, 18), (5, 3, 9), (3, 3, 5), (3, 3, 3)]
+    assert level_dims((3, 3, 3), 0) == [(3, 3, 3)]
+    per = level_dims((320, 320, 320), 3)
+    assert per[-1] == (3, 10, 10)
+    assert all(d[1] % 2 == 0 and d[2] % 2 == 0 for d in per)
+    assert level_dims((14, 12, 16), 3) == [(14, 12, 16), (7, 6, 8), (4, 6, 4), (2, 6, 2)]
+    for dims, p in [((100, 37, 9), 0), ((64, 48, 80), 3), ((5, 200, 6), 1)]:
+        lv = level_dims(dims, p)
+        for f, c in zip(lv, lv[1:]):
+            assert all(cc in (ff, (ff + 1) // 2) for ff, cc in zip(f, c))
+        assert level_dims(lv[-1], p) == [lv[-1]]
