@@ -314,3 +314,21 @@ def test_multigrid_on_thin_tiny_and_batched_shapes(shape, periodic):
     d64, _, _ = d_eff_fp64(OracleSolve(kap, kind="periodic_kappa" if periodic else "kappa"), rtol=1e-12,
                            coefficients="f64")
     np.testing.assert_allclose(s.D_eff, d64, rtol=1e-9)
+
+
+def test_multigrid_refinement_with_a_non_percolating_volume():
+    """A batch whose second volume has no path from x = 0 to x = nx - 1 (its clusters are all
+    frozen in the anchored system): the multigrid correction still reaches the tolerance, the
+    first volume's D_eff matches the FP64 oracle and the second reports tau = inf."""
+    from cases import random_binary
+
+    live = random_binary((20, 16, 24), 107, 0.7)
+    dead = random_binary((20, 16, 24), 108, 0.7)
+    dead[9:11] = 0  # a solid slab across x
+    img = np.stack([live, dead])
+    s = tg.Solver(img)
+    s.solve(verbose=False, conv_crit=1e-3, refine={"tol": 1e-11, "inner": "mg"})
+    assert s.residual_history[-1] < 1e-11 and not s.inner_fallback
+    d64, _, _ = d_eff_fp64(OracleSolve(live[None], kind="binary"), rtol=1e-11)
+    np.testing.assert_allclose(s.D_eff[0], d64[0], rtol=1e-8)
+    assert np.isinf(s.tau[1])
