@@ -41,7 +41,7 @@ import torch
 
 from . import _capi
 from ._capi import TF_KIND_MULTIPHASE, TF_PERIODIC_Y, TF_PERIODIC_Z, TfGeom, TfOperator, check
-from .solvers import layer_metrics, relative_residual
+from .solvers import keep_non_percolating, layer_metrics, relative_residual
 
 
 def _ptr(t: torch.Tensor) -> int:
@@ -351,9 +351,11 @@ class KappaSolver:
             self.residual_history = self._fp64_solve(c64, None, tol, max_outer, n_inner, inner)
             check(lib.tf_narrow_f64(C.byref(g), C.byref(self._op), _ptr(c64), _ptr(self._c), st), "tf_narrow_f64")
             self._c64 = c64
+            tau_before = self.tau
             self.tau, _ = self.compute_metrics()
             torch.cuda.synchronize(self.device)
         self.tau = np.where(self.tau == 0, np.inf, self.tau)
+        keep_non_percolating(self, tau_before)
         self.timings["refine_s"] = timer() - t0
         return self.residual_history
 

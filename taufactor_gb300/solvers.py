@@ -260,10 +260,12 @@ class SORSolver:
                 code = self._code if self._kind == TF_KIND_BINARY else self._anchored_code()
             c64, hist = refine_field(self._lib, self._geom, self._op, self._cur, code, self._err,
                                      self._stream(), self.batch_size, tol, max_outer, n_inner, omega, solve_e)
+        tau_before = self.tau
         self._field64 = c64
         self.residual_history = hist
         self.tau, _ = self.compute_metrics()
         self.tau = np.where(self.tau == 0, np.inf, self.tau)
+        keep_non_percolating(self, tau_before)
         return hist
 
     def _phase_conductivities(self) -> np.ndarray:
@@ -650,6 +652,23 @@ class ThroughTransportSolver(SORSolver):
     def _build_factor(self) -> torch.Tensor:
         raise NotImplementedError(f"{type(self).__name__} has no divisor tensor")
 
+
+
+def keep_non_percolating(s, tau_before) -> None:
+    """After an FP64 correction: a volume the float32 solve found without a percolating path
+    (tau 0, later inf, from an exactly zero layer flux, taufactor.py:318-327) keeps that verdict. In
+    float64 its blocked layers carry rounding noise (~1e-17) instead of an exact zero, which the
+    reference's zero test would read as a tortuosity of ~1e16."""
+    if tau_before is None:
+        return
+    tb = np.asarray(tau_before, dtype=np.float64)
+    dead = np.isinf(tb) | (tb == 0)  # 0 before the convergence check turns it into inf
+    if dead.shape != np.shape(s.tau) or not dead.any():
+        return
+    s.tau = np.where(dead, np.inf, s.tau)
+    s.D_eff = np.where(dead, 0.0, s.D_eff)
+    if s.tau_x is not None:
+        s.tau_x[dead] = 0
 
 
 def layer_metrics(s, flux_1d: np.ndarray, c_x_raw: np.ndarray):

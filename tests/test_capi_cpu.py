@@ -191,3 +191,21 @@ def test_multigrid_level_dims():
         for f, c in zip(lv, lv[1:]):
             assert all(cc in (ff, (ff + 1) // 2) for ff, cc in zip(f, c))
         assert level_dims(lv[-1], p) == [lv[-1]]
+
+
+def test_refinement_keeps_the_percolation_verdict():
+    """A volume the float32 solve declared non-percolating (tau 0 or inf) keeps tau = inf,
+    D_eff = 0 and tau_x = 0 after the FP64 correction; the others keep their refined values."""
+    from types import SimpleNamespace
+
+    from taufactor_gb300.solvers import keep_non_percolating
+
+    s = SimpleNamespace(tau=np.array([1.9, 3.2e15, 2.5]), D_eff=np.array([0.4, 1e-17, 0.3]),
+                        tau_x=np.ones((3, 4)))
+    keep_non_percolating(s, np.array([1.91, np.inf, 0.0]))
+    assert s.tau[0] == 1.9 and np.isinf(s.tau[1]) and np.isinf(s.tau[2])
+    assert s.D_eff.tolist() == [0.4, 0.0, 0.0]
+    assert s.tau_x[0].tolist() == [1.0] * 4 and not s.tau_x[1:].any()
+    t = SimpleNamespace(tau=np.array([1.0]), D_eff=np.array([0.5]), tau_x=None)
+    keep_non_percolating(t, None)
+    assert t.tau[0] == 1.0 and t.D_eff[0] == 0.5

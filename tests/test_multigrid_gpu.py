@@ -317,9 +317,10 @@ def test_multigrid_on_thin_tiny_and_batched_shapes(shape, periodic):
 
 
 def test_multigrid_refinement_with_a_non_percolating_volume():
-    """A batch whose second volume has no path from x = 0 to x = nx - 1 (its clusters are all
-    frozen in the anchored system): the multigrid correction still reaches the tolerance, the
-    first volume's D_eff matches the FP64 oracle and the second reports tau = inf."""
+    """A batch whose second volume has no path from x = 0 to x = nx - 1 (a solid slab across x;
+    the reference's exact-zero test does not catch it, its layer fluxes keep their signs): the
+    multigrid correction still reaches the tolerance, the first volume's D_eff matches the FP64
+    oracle and the blocked volume's float64 D_eff is zero to rounding."""
     from cases import random_binary
 
     live = random_binary((20, 16, 24), 107, 0.7)
@@ -331,4 +332,4 @@ def test_multigrid_refinement_with_a_non_percolating_volume():
     assert s.residual_history[-1] < 1e-11 and not s.inner_fallback
     d64, _, _ = d_eff_fp64(OracleSolve(live[None], kind="binary"), rtol=1e-11)
     np.testing.assert_allclose(s.D_eff[0], d64[0], rtol=1e-8)
-    assert np.isinf(s.tau[1])
+    assert abs(s.D_eff[1]) < 1e-12 * abs(s.D_eff[0])
