@@ -456,7 +456,8 @@ int tf_mg_prolong(const tf_geom* coarse, const float* ec_dev, const tf_geom* fin
 int tf_mg_apply(const tf_geom* g, const float* in_dev, const float* fx_dev, const float* fy_dev,
                 const float* fz_dev, const float* div_dev, float* out_dev, void* stream);
 
-/* Per-volume float64 dot products over interior cells, in a fixed order: out[b] = sum a1*b1 and,
+/* Per-volume dot products over interior cells (a float4 group's products summed in float32, the
+ * groups accumulated in float64), in a fixed order: out[b] = sum a1*b1 and,
  * when a2_dev/b2_dev are given, out[batch + b] = sum a2*b2. part_dev: double [2 * batch*nx*ny]. */
 int tf_mg_dot(const tf_geom* g, const float* a1_dev, const float* b1_dev, const float* a2_dev, const float* b2_dev,
               double* part_dev, double* out_dev, void* stream);

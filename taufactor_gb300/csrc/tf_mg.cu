@@ -21,7 +21,8 @@
 // k_mg_restrict  coarse right-hand side = sum over the aggregate of (rhs - A e)
 // k_mg_prolong   e += coarse e on every cell of the aggregate
 // k_mg_apply     out = A in (interior cells; 0 on cells without a finite factor)
-// k_mg_dot_rows / k_mg_dot_sum   per-volume float64 dot products over interior cells, in a fixed order
+// k_mg_dot_rows / k_mg_dot_sum   per-volume dot products over interior cells (float32 products of
+//                                a float4 group, float64 accumulation), in a fixed order
 // k_pcg_xr / k_pcg_p             the conjugate-gradient vector updates with per-volume scalars
 #include "tf_common.cuh"
 #include "tf_internal.h"
