@@ -209,3 +209,37 @@ def test_refinement_keeps_the_percolation_verdict():
     t = SimpleNamespace(tau=np.array([1.0]), D_eff=np.array([0.5]), tau_x=None)
     keep_non_percolating(t, None)
     assert t.tau[0] == 1.0 and t.D_eff[0] == 0.5
+
+
+def test_multigrid_and_kappa_entry_points_refuse_bad_arguments(lib):
+    """The multigrid, float64-face and fused-sweep entry points check their arguments before
+    any launch: levels that are not a coarsening of each other, missing or misaligned buffers,
+    one field passed as both ping-pong buffers, a second dot product without its partner."""
+    f, c, wrong = _capi.TfGeom(), _capi.TfGeom(), _capi.TfGeom()
+    lib.tf_geometry(1, 16, 12, 10, 0, C.byref(f))
+    lib.tf_geometry(1, 8, 6, 5, 0, C.byref(c))
+    lib.tf_geometry(1, 8, 5, 5, 0, C.byref(wrong))  # 12 -> 5 is no halving
+    op = _capi.TfOperator()
+    op.omega = 1.0
+    n0 = lib.tf_launch_count()
+    P = 4096  # a 16-byte aligned stand-in pointer; nothing is dereferenced on refusal
+    assert lib.tf_mg_coarsen(C.byref(f), P, P, P, C.byref(wrong), P, P, P, P, 0, 0.5, None) == _capi.TF_ERR_ARG
+    assert lib.tf_mg_coarsen(C.byref(f), P, P, P, C.byref(c), P, P, P, P, 0, 0.0, None) == _capi.TF_ERR_ARG
+    assert lib.tf_mg_coarsen(C.byref(f), None, P, P, C.byref(c), P, P, P, P, 0, 0.5, None) == _capi.TF_ERR_ARG
+    assert lib.tf_mg_restrict(C.byref(f), P, P, P, P, P, P, C.byref(wrong), P, None) == _capi.TF_ERR_ARG
+    assert lib.tf_mg_prolong(C.byref(wrong), P, C.byref(f), P, 0, None) == _capi.TF_ERR_ARG
+    assert lib.tf_mg_apply(C.byref(f), P + 4, P, P, P, P, P, None) == _capi.TF_ERR_ARG  # misaligned
+    assert lib.tf_mg_dot(C.byref(f), P, P, P, None, P, P, None) == _capi.TF_ERR_ARG
+    assert lib.tf_pcg_update_xr(C.byref(f), P, P, P, None, P, P, None) == _capi.TF_ERR_ARG
+    assert lib.tf_pcg_update_p(C.byref(f), P + 8, P, P, P, None) == _capi.TF_ERR_ARG
+    assert lib.tf_kappa_faces_f64(C.byref(f), None, P, P, P, P, None) == _capi.TF_ERR_ARG
+    assert lib.tf_kappa_residual_faces_f64(C.byref(f), C.byref(op), P, P, P, P, None, None, P, P, P, None) == \
+        _capi.TF_ERR_ARG
+    res = C.c_int(0)
+    assert lib.tf_kappa_advance_fused(C.byref(f), C.byref(op), P, P, P, P, P, P, None, 0, 4, None, C.byref(res),
+                                      None) == _capi.TF_ERR_ARG  # the same buffer twice
+    assert lib.tf_kappa_advance_fused(C.byref(f), C.byref(op), P, P + 16, P, P, P, P, P + 4, 0, 4, None,
+                                      C.byref(res), None) == _capi.TF_ERR_ARG  # misaligned rhs
+    assert lib.tf_refresh_ghosts(C.byref(f), 3, None, None) == _capi.TF_ERR_ARG
+    assert lib.tf_refresh_ghosts(C.byref(f), 0, P, None) == _capi.TF_OK  # nothing to do, no launch
+    assert lib.tf_launch_count() == n0
