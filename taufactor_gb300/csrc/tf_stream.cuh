@@ -244,6 +244,15 @@ __device__ __forceinline__ void stream_tile(const CUtensorMap* tmf, const CUtens
     for (int s = 1; s <= K; ++s) stage_rows |= (ty >= s && ty < ROWS - s) ? (1u << s) : 0u;
     const bool py = a.periodic & TF_PERIODIC_Y, pz = a.periodic & TF_PERIODIC_Z;
 
+    // write-back invariants: this thread's interior group (if any), its row in plane 0 of the
+    // output, and whether both half-row groups are whole and need no periodic ghost copy (the
+    // common case: one pointer select and one 128-bit store per half-row and step)
+    const int jw = j0 + 4 * (gi - 1);
+    const bool writes = interior_group && ty >= K && ty < K + TY && y < g.NY;
+    const bool wb_plain = writes && jw + 4 <= half_len(g.NZ, 1) && !(py && (y < HY || y >= g.NY - HY)) &&
+                          !(pz && (jw < HJ || jw + 4 > (g.NZ >> 1) - HJ));
+    float* const wb_row = a.out + (long long)b * g.vol_f + (long long)(y + HY) * g.row_f + HJ + jw;
+
     // steps: the last chunk runs K past the volume (Dirichlet plane NX), the others stop at xe
     const int total = xe == NX ? NX + K : xe;
     for (int t0 = xs; t0 < total; t0 += R) {
@@ -331,11 +340,17 @@ __device__ __forceinline__ void stream_tile(const CUtensorMap* tmf, const CUtens
                 // write back plane t-K from registers
                 const int pw = t - K;
                 const int iw = (i - K + 2 * R) % R;
-                if (pw >= x0 && pw < x1 && interior_group && ty >= K && ty < K + TY && y < g.NY) {
+                if (pw >= x0 && pw < x1 && wb_plain) {
+                    // V0 holds relative colour 0: the even-z half-row when pw + y + c0 is even
+                    float* const wp = wb_row + (long long)pw * g.plane_f;
+                    const bool even0 = ((pw + y + c0) & 1) == 0;
+                    st4(even0 ? wp : wp + g.ZH, V0[iw]);
+                    st4(even0 ? wp + g.ZH : wp, V1[iw]);
+                } else if (pw >= x0 && pw < x1 && writes) {
                     const bool even0 = ((pw + y + c0) & 1) == 0;
                     const float4 ev = even0 ? V0[iw] : V1[iw];
                     const float4 od = even0 ? V1[iw] : V0[iw];
-                    const int j = j0 + 4 * (gi - 1);
+                    const int j = jw;
                     float* outp = a.out + (long long)b * g.vol_f + (long long)pw * g.plane_f;
 #pragma unroll
                     for (int q = 0; q < 2; ++q) {
