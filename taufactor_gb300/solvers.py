@@ -999,12 +999,15 @@ class MultiPhaseSolver(ThroughTransportSolver):
         factor[factor == 0] = torch.inf
         return factor
 
-    def phase_gradients(self, conv_crit: float = 1e-3, tol: float = 1e-11) -> dict:
+    def phase_gradients(self, conv_crit: float = 1e-3, tol: float = 1e-11, method: str = "mg") -> dict:
         """dD_eff/dD_p for every label p (numpy [B] per label), by the adjoint method.
 
         Builds the per-voxel field kappa = D[label] (float32, the same faces as this solver,
-        bit for bit), solves it to the reference's rule plus FP64 defect correction, solves the
-        adjoint and sums dD_eff/dkappa over the voxels of each label. The derivative is that of
+        bit for bit), solves it to an FP64 relative residual of tol, solves the adjoint and sums
+        dD_eff/dkappa over the voxels of each label. method "mg" (default): the FP64 defect
+        correction with multigrid inner solves from the initial field (conv_crit is not used);
+        "sor": the reference's float32 loop to conv_crit first, then the correction. Only the
+        corrected field enters the gradient, so both give it to tol. The derivative is that of
         the operator with float64 faces 2ab/(a+b) (KappaSolver's default): with float32 faces
         D_eff moves in rounding steps. For a label of conductivity 0 the value is not a
         derivative (the label's voxels are outside the system there). No reference counterpart
@@ -1020,7 +1023,7 @@ class MultiPhaseSolver(ThroughTransportSolver):
         lut = np.array([F32(self.Ds.get(int(p), 0.0)) for p in labels], dtype=np.float32)
         kap = torch.from_numpy(np.ascontiguousarray(lut[idx])).to(self.device)
         ks = KappaSolver(kap, periodic=bool(self._periodic), omega=self.omega, D_0=self.D_0, device=self.device)
-        ks.solve(conv_crit=conv_crit, refine={"tol": tol})
+        ks.solve(conv_crit=conv_crit, refine={"tol": tol}, method=method)
         g = ks.gradient(tol=tol).cpu().numpy()
         self.kappa_solver = ks
         sums = np.stack([np.bincount(idx[b].ravel(), weights=g[b].ravel(), minlength=len(labels))
