@@ -104,6 +104,17 @@ int tf_label_stats(int batch, int nx, int ny, int nz, const uint8_t* labels_dev,
 int tf_kappa_stats(int batch, int nx, int ny, int nz, const float* kappa_dev, uint64_t* plane_positive_dev,
                    double* plane_sums_dev, int32_t* bad_dev, void* stream);
 
+/* out[i] = table[labels[i]] for n voxels: uint8 labels, a 256-entry float32 table, float32 out,
+ * all in device memory (MultiPhaseSolver.phase_gradients: the conductivity field D[label]). */
+int tf_label_map(const uint8_t* labels_dev, long long n, const float* table_dev, float* out_dev, void* stream);
+
+/* Per-plane float64 sums of values_dev (float64 [batch][nx][ny][nz]) over the voxels of each label
+ * slot: plane_sums_dev[(b * nx + x) * n_slots + s] = sum of the values whose label l has
+ * slot_of_dev[l] == s (int32 [256]; -1 = no slot). One CTA per plane in a fixed order
+ * (MultiPhaseSolver.phase_gradients: dD_eff/dD_p as the sum of dD_eff/dkappa over label p). */
+int tf_label_sums(int batch, int nx, int ny, int nz, const uint8_t* labels_dev, const double* values_dev,
+                  const int32_t* slot_of_dev, int n_slots, double* plane_sums_dev, void* stream);
+
 /* Build the code buffer and the initial field from per-voxel phase indices.
  * Replaces ThroughTransportSolver.init_field + _pad (taufactor.py:282-291, :228-238),
  * Solver/PeriodicSolver/AnisotropicSolver.init_conductive_neighbours (:402-410, :493-499,

@@ -32,7 +32,7 @@ EXPORTS = (
     "tf_kappa_stats", "tf_mg_coarsen", "tf_mg_restrict", "tf_mg_prolong", "tf_mg_apply", "tf_mg_dot",
     "tf_pcg_update_xr", "tf_pcg_update_p", "tf_kappa_faces_f64", "tf_kappa_residual_faces_f64",
     "tf_kappa_layer_sums_faces_f64", "tf_kappa_gradient_faces_f64", "tf_kappa_advance_fused",
-    "tf_refresh_ghosts",
+    "tf_refresh_ghosts", "tf_label_map", "tf_label_sums",
 )
 TF_IMP_TABLE = 56
 TF_BATCH_ACTIVE, TF_BATCH_CONVERGED, TF_BATCH_NEEDS_HOST = 0, 1, 2
@@ -111,6 +111,8 @@ def load():
         "tf_batch_advance_tile": (i32, [vp, vp, i32, vp, i32, i32, vp]),
         "tf_label_stats": (i32, [i32, i32, i32, i32, vp, vp, vp, vp]),
         "tf_kappa_stats": (i32, [i32, i32, i32, i32, vp, vp, vp, vp, vp]),
+        "tf_label_map": (i32, [vp, i64, vp, vp, vp]),
+        "tf_label_sums": (i32, [i32, i32, i32, i32, vp, vp, vp, i32, vp, vp]),
         "tf_anchored_phase": (i32, [i32, i32, i32, i32, i32, vp, vp, vp, vp, vp, vp, vp]),
         "tf_batch_advance_rhs_tile": (i32, [vp, vp, i32, vp, i32, i32, vp]),
         "tf_batch_layer_sums": (i32, [vp, vp, i32, vp, i32, vp, vp, vp]),

@@ -152,3 +152,80 @@ extern "C" int tf_kappa_stats(int batch, int nx, int ny, int nz, const float* ka
     note_launch();
     return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
 }
+
+// Per-voxel lookup of a 256-entry float32 table by uint8 label (MultiPhaseSolver.phase_gradients:
+// the conductivity field kappa = D[label]), and per-plane float64 sums of a field over the voxels
+// of each label (the per-label sums of dD_eff/dkappa). One thread per voxel in a grid-stride loop
+// for the lookup; one CTA per plane for the sums, four label slots per pass accumulated in
+// registers and reduced by shuffles and a fixed warp order, so the sums do not depend on
+// scheduling.
+namespace tf {
+
+__global__ void __launch_bounds__(256) k_label_map(const uint8_t* __restrict__ labels, long long n,
+                                                   const float* __restrict__ table, float* __restrict__ out) {
+    __shared__ float s_t[256];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) s_t[i] = table[i];
+    __syncthreads();
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = s_t[labels[i]];
+}
+
+__global__ void __launch_bounds__(256) k_label_sums(const uint8_t* __restrict__ labels,
+                                                    const double* __restrict__ values, long long plane_elems,
+                                                    const int32_t* __restrict__ slot_of, int n_slots,
+                                                    double* __restrict__ sums) {
+    __shared__ int s_slot[256];
+    __shared__ double s_red[8][4];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) s_slot[i] = slot_of[i];
+    __syncthreads();
+    const long long plane = blockIdx.x;
+    const uint8_t* lab = labels + plane * plane_elems;
+    const double* val = values + plane * plane_elems;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (int s0 = 0; s0 < n_slots; s0 += 4) {
+        double acc[4] = {0.0, 0.0, 0.0, 0.0};
+        for (long long i = threadIdx.x; i < plane_elems; i += blockDim.x) {
+            const int k = s_slot[lab[i]] - s0;
+            const double v = val[i];
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+                if (k == j) acc[j] += v;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            for (int o = 16; o > 0; o >>= 1) acc[j] += __shfl_down_sync(0xffffffffu, acc[j], o);
+            if (lane == 0) s_red[warp][j] = acc[j];
+        }
+        __syncthreads();
+        if (threadIdx.x < 4 && s0 + (int)threadIdx.x < n_slots) {
+            double t = 0.0;
+            for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += s_red[w][threadIdx.x];
+            sums[plane * n_slots + s0 + threadIdx.x] = t;
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace tf
+
+extern "C" int tf_label_map(const uint8_t* labels_dev, long long n, const float* table_dev, float* out_dev,
+                            void* stream) {
+    if (n < 1 || !labels_dev || !table_dev || !out_dev) return TF_ERR_ARG;
+    const long long blocks = (n + 255) / 256 < 16LL * sm_count() ? (n + 255) / 256 : 16LL * sm_count();
+    k_label_map<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(labels_dev, n, table_dev, out_dev);
+    note_launch();
+    return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
+}
+
+extern "C" int tf_label_sums(int batch, int nx, int ny, int nz, const uint8_t* labels_dev, const double* values_dev,
+                             const int32_t* slot_of_dev, int n_slots, double* plane_sums_dev, void* stream) {
+    if (batch < 1 || nx < 1 || ny < 1 || nz < 1 || n_slots < 1 || n_slots > 256 || !labels_dev || !values_dev ||
+        !slot_of_dev || !plane_sums_dev)
+        return TF_ERR_ARG;
+    const long long planes = (long long)batch * nx;
+    if (planes > 0x7fffffffLL) return TF_ERR_UNSUPPORTED;
+    k_label_sums<<<(unsigned)planes, 256, 0, (cudaStream_t)stream>>>(labels_dev, values_dev, (long long)ny * nz,
+                                                                      slot_of_dev, n_slots, plane_sums_dev);
+    note_launch();
+    return cudaGetLastError() == cudaSuccess ? TF_OK : TF_ERR_CUDA;
+}

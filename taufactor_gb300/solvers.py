@@ -1015,19 +1015,44 @@ class MultiPhaseSolver(ThroughTransportSolver):
         """
         from .kappa import KappaSolver
 
-        # kappa = D[label] and the per-label sums of the gradient on the host (a lookup table and
-        # a bincount over the labels), so no torch reduction or mask kernels join the GPU path
-        labels = unique_labels(self.cpu_img)
+        labels = self._labels
         img = np.asarray(self.cpu_img)
-        idx = np.searchsorted(labels, img)  # label -> position in `labels`
-        lut = np.array([F32(self.Ds.get(int(p), 0.0)) for p in labels], dtype=np.float32)
-        kap = torch.from_numpy(np.ascontiguousarray(lut[idx])).to(self.device)
-        ks = KappaSolver(kap, periodic=bool(self._periodic), omega=self.omega, D_0=self.D_0, device=self.device)
-        ks.solve(conv_crit=conv_crit, refine={"tol": tol}, method=method)
-        g = ks.gradient(tol=tol).cpu().numpy()
-        self.kappa_solver = ks
-        sums = np.stack([np.bincount(idx[b].ravel(), weights=g[b].ravel(), minlength=len(labels))
-                         for b in range(g.shape[0])])
+        B, X, Y, Z = img.shape
+        lib = _capi.load()
+        on_device = img.dtype == np.uint8
+        with torch.cuda.device(self.device):
+            st = torch.cuda.current_stream(self.device).cuda_stream
+            if on_device:
+                # uint8 labels: kappa = D[label] by a 256-entry table and the per-label sums of the
+                # gradient on the device (tf_label_map, tf_label_sums)
+                table = np.zeros(256, dtype=np.float32)
+                slot = np.full(256, -1, dtype=np.int32)
+                for i, p in enumerate(labels):
+                    table[int(p)] = F32(self.Ds.get(int(p), 0.0))
+                    slot[int(p)] = i
+                lab = torch.from_numpy(img).to(self.device)
+                table_d, slot_d = torch.from_numpy(table).to(self.device), torch.from_numpy(slot).to(self.device)
+                kap = torch.empty(img.shape, dtype=torch.float32, device=self.device)
+                check(lib.tf_label_map(lab.data_ptr(), lab.numel(), table_d.data_ptr(), kap.data_ptr(), st),
+                      "tf_label_map")
+            else:
+                # other label types: the same table through positions in `labels`, on the host
+                idx = np.searchsorted(labels, img)
+                lut = np.array([F32(self.Ds.get(int(p), 0.0)) for p in labels], dtype=np.float32)
+                kap = torch.from_numpy(np.ascontiguousarray(lut[idx])).to(self.device)
+            ks = KappaSolver(kap, periodic=bool(self._periodic), omega=self.omega, D_0=self.D_0, device=self.device)
+            ks.solve(conv_crit=conv_crit, refine={"tol": tol}, method=method)
+            g = ks.gradient(tol=tol)
+            self.kappa_solver = ks
+            if on_device:
+                part = torch.empty((B * X, len(labels)), dtype=torch.float64, device=self.device)
+                check(lib.tf_label_sums(B, X, Y, Z, lab.data_ptr(), g.contiguous().data_ptr(), slot_d.data_ptr(),
+                                        len(labels), part.data_ptr(), st), "tf_label_sums")
+                sums = part.cpu().numpy().reshape(B, X, len(labels)).sum(axis=1)
+            else:
+                gh = g.cpu().numpy()
+                sums = np.stack([np.bincount(idx[b].ravel(), weights=gh[b].ravel(), minlength=len(labels))
+                                 for b in range(B)])
         return {int(p): sums[:, i] for i, p in enumerate(labels)}
 
 

@@ -158,6 +158,21 @@ def test_multiphase_phase_gradients_match_finite_differences():
         assert abs(fd - grads[p][0]) / abs(fd) < 1e-3, (p, fd, grads[p][0])
 
 
+def test_phase_gradients_device_labels_match_host_labels():
+    """uint8 labels take the device path (tf_label_map, tf_label_sums); the same labels as int64
+    take the host path: the same kappa field, so the same solve, and per-label sums equal to
+    float64 rounding."""
+    lab = random_labels((2, 12, 10, 14), 67)
+    ds = {0: 0.3, 1: 1.0, 2: 0.05}
+    a = tg.MultiPhaseSolver(lab, dict(ds))
+    b = tg.MultiPhaseSolver(lab.astype(np.int64), dict(ds))
+    ga = a.phase_gradients(tol=1e-12)
+    gb = b.phase_gradients(tol=1e-12)
+    assert torch.equal(a.kappa_solver.kappa, b.kappa_solver.kappa)
+    for p in ds:
+        np.testing.assert_allclose(ga[p], gb[p], rtol=1e-12, atol=1e-15)
+
+
 def test_kappa_set_up_statistics_and_input_check():
     """vol_x and D_mean come from one device pass (tf_kappa_stats) and match the host
     computation; negative, infinite and NaN conductivities are refused."""

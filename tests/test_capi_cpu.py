@@ -243,3 +243,17 @@ def test_multigrid_and_kappa_entry_points_refuse_bad_arguments(lib):
     assert lib.tf_refresh_ghosts(C.byref(f), 3, None, None) == _capi.TF_ERR_ARG
     assert lib.tf_refresh_ghosts(C.byref(f), 0, P, None) == _capi.TF_OK  # nothing to do, no launch
     assert lib.tf_launch_count() == n0
+
+
+def test_label_map_and_sums_refuse_bad_arguments(lib):
+    """tf_label_map and tf_label_sums check their arguments before any launch."""
+    n0 = lib.tf_launch_count()
+    P = 1 << 20  # a non-null address that is never dereferenced: every call below is refused
+    assert lib.tf_label_map(None, 10, P, P, None) == _capi.TF_ERR_ARG
+    assert lib.tf_label_map(P, 0, P, P, None) == _capi.TF_ERR_ARG
+    assert lib.tf_label_map(P, 10, P, None, None) == _capi.TF_ERR_ARG
+    assert lib.tf_label_sums(1, 4, 4, 4, P, P, P, 0, P, None) == _capi.TF_ERR_ARG  # no slots
+    assert lib.tf_label_sums(1, 4, 4, 4, P, P, P, 257, P, None) == _capi.TF_ERR_ARG
+    assert lib.tf_label_sums(0, 4, 4, 4, P, P, P, 3, P, None) == _capi.TF_ERR_ARG
+    assert lib.tf_label_sums(1, 4, 4, 4, P, None, P, 3, P, None) == _capi.TF_ERR_ARG
+    assert lib.tf_launch_count() == n0
