@@ -33,7 +33,7 @@ extern "C" {
 #define TF_ERR_ARG 1         /* invalid argument (shape, pointer, alignment, sizes)        */
 #define TF_ERR_CUDA 2        /* a CUDA runtime call failed                                 */
 #define TF_ERR_TIMEOUT 3     /* a bounded device-side wait ran out; kernel returned early   */
-#define TF_ERR_UNSUPPORTED 4 /* valid request this build does not handle                    */
+#define TF_ERR_UNSUPPORTED 4 /* valid request the library does not handle                   */
 #define TF_ERR_NOTCONV 5     /* iteration limit reached before convergence                  */
 
 /* operator kinds */

@@ -154,7 +154,7 @@ def test_validation_errors_match_reference():
 
 
 def test_no_cpu_fallback():
-    """The reference falls back to the CPU; this build refuses."""
+    """The reference falls back to the CPU; this package refuses."""
     with pytest.raises(RuntimeError, match="CUDA"):
         Solver(np.ones((4, 4, 4)), device="cpu")
 
