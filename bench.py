@@ -7,9 +7,10 @@ field. Inputs (1.07 GB of field) exceed L2, so no flush is needed between steps.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-``--impl reference`` times the reference algorithm on the host cores (the oracle's float32
-restatement in numpy, one process per volume) on a bounded sample of the same workload.
-Under torchrun every rank solves its own batch (weak scaling, no data-path collective).
+``--impl reference`` times the reference's own CPU Solver (installed under baseline/_ref) on the
+host cores, on a bounded sample of the same workload; without the installed reference, the
+oracle's float32 restatement in numpy. Under torchrun every rank solves its own batch (weak
+scaling, no data-path collective).
 """
 from __future__ import annotations
 
@@ -35,7 +36,7 @@ CONV_CRIT = 1e-4
 CPU_SAMPLE_HALF_SWEEPS = 10
 # DRAM bytes per voxel moved by one launch of the fused sweep (16x128 tile, 4 half-sweeps):
 # dram__bytes_read.sum + dram__bytes_write.sum from one ncu capture on 4 x 256^3 blurred-noise
-# volumes (645 MB for 67.1 M voxels); traffic grows in proportion to the voxels processed.
+# volumes (645–647 MB for 67.1 M voxels); traffic grows in proportion to the voxels processed.
 TRAFFIC_BYTES_PER_VOXEL_LAUNCH = 645.2e6 / (4 * 256 ** 3)
 
 
@@ -980,6 +981,19 @@ def run_profile(args):
         torch.cuda.synchronize()
         print(f"profile workload done: impedance {args.side}^3, {args.half_sweeps} half-sweeps")
         return
+    if args.electrode:  # ElectrodeSolver on --batch three-label --side^3 volumes (electrode_throughput's)
+        from scipy.ndimage import gaussian_filter
+
+        rngs = [np.random.default_rng(4000 + i) for i in range(args.batch)]
+        vols = np.stack([np.argmax(np.stack([gaussian_filter(r.standard_normal((args.side,) * 3, dtype=np.float32), 2.0)
+                                             for _ in range(3)]), axis=0).astype(np.uint8) for r in rngs])
+        s = tg.ElectrodeSolver(vols, device="cuda")
+        s._advance(8)
+        torch.cuda.synchronize()
+        s._advance(args.half_sweeps)
+        torch.cuda.synchronize()
+        print(f"profile workload done: electrode {args.batch}x{args.side}^3, {args.half_sweeps} half-sweeps")
+        return
     if args.multiphase:  # MultiPhaseSolver on the three-label --side^3 volume, --half-sweeps half-sweeps
         from taufactor_gb300.synthetic import three_phase
 
@@ -1040,6 +1054,8 @@ def main():
     ap.add_argument("--multigrid", action="store_true",
                     help="--profile: one multigrid-PCG FP64 correction of a --side^3 kappa field")
     ap.add_argument("--impedance", action="store_true", help="--profile: ImpedanceSolver on one volume")
+    ap.add_argument("--electrode", action="store_true",
+                    help="--profile: ElectrodeSolver on --batch three-label --side^3 volumes")
     ap.add_argument("--uneven", action="store_true", help="--profile: one batched solve of the uneven batch")
     ap.add_argument("--workload", choices=["uneven", "adjoint", "design", "electrode", "impedance"], default=None,
                     help="print the secondary measurement of this workload only")
