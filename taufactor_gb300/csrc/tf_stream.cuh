@@ -200,7 +200,7 @@ __device__ __forceinline__ void stream_tile(const CUtensorMap* tmf, const CUtens
     }
     if (KIND == TF_KIND_ANISOTROPIC)
         for (int i = tid; i < 256; i += NT) lut[i] = op->divisor[i];
-    if (KIND == TF_KIND_ELECTRODE && tid == 0) lut[0] = op->divisor[b & 255];  // k_0 of volume b
+    if (KIND == TF_KIND_ELECTRODE) fill_electrode_divisors(lut, op->divisor[b & 255], tid, NT);  // k_0 of volume b
     if (KIND == TF_KIND_MULTIPHASE)
         for (int i = tid; i < 32 * 32; i += NT) lut[i] = op->face[i];
     if (KIND == TF_KIND_BINARY) fill_division_table(tab_all, tid, NT);

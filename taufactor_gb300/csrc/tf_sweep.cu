@@ -26,7 +26,8 @@ __global__ void __launch_bounds__(256) k_plain(float* __restrict__ f, const uint
     __shared__ float4 tab[DIV_PAIRS * DIV_COPIES];
     if (KIND == TF_KIND_ANISOTROPIC)
         for (int i = threadIdx.x; i < 256; i += blockDim.x) lut[i] = op.divisor[i];
-    if (KIND == TF_KIND_ELECTRODE && threadIdx.x == 0) lut[0] = op.divisor[(blockIdx.z / a.g.NX) & 255];
+    if (KIND == TF_KIND_ELECTRODE)
+        fill_electrode_divisors(lut, op.divisor[(blockIdx.z / a.g.NX) & 255], threadIdx.x, blockDim.x);
     if (KIND == TF_KIND_MULTIPHASE)
         for (int i = threadIdx.x; i < 32 * 32; i += blockDim.x) lut[i] = op.face[i];
     if (KIND == TF_KIND_BINARY) fill_division_table(tab, threadIdx.x, blockDim.x);

@@ -84,6 +84,20 @@ __device__ __forceinline__ void fill_division_table(float4* tab, int tid, int nt
         tab[i] = make_float4(-nl, -nh, lo ? __frcp_rn(nl) : 0.0f, hi ? __frcp_rn(nh) : 0.0f);
     }
 }
+// Electrode operator: the divisor of every code of one volume into lut[0..255]. code = 1 + nn +
+// 8 nr (0: not conductive); factor nn + nr * k_0 in float32 as the reference forms it
+// (electrode.py:46-62, taufactor.py:47-55), inf where it is 0 or the voxel is not conductive.
+__device__ __forceinline__ void fill_electrode_divisors(float* lut, float k0, int tid, int nthreads) {
+    for (int i = tid; i < 256; i += nthreads) {
+        float d = __int_as_float(0x7f800000);
+        if (i != 0) {
+            const uint32_t m = (uint32_t)i - 1u;
+            const float f = __fadd_rn(static_cast<float>(m & 7u), __fmul_rn(static_cast<float>(m >> 3), k0));
+            if (f != 0.0f) d = f;
+        }
+        lut[i] = d;
+    }
+}
 // This thread's copy of the table (copy lane % 8).
 __device__ __forceinline__ const float4* division_copy(const float4* tab) { return tab + (threadIdx.x & 7); }
 
@@ -180,22 +194,16 @@ __device__ __forceinline__ float4 update4(float4 c, const float4& xp, const floa
         float sum, quot;
         if (KIND == TF_KIND_ELECTRODE) {
             // the default neighbour sum (taufactor.py:95-103) over the divisor
-            // factor = nn + nr * k_0 in float32, inf where 0 (:47-55, electrode.py:46-62);
-            // lut[0] = k_0 of this volume, code = 1 + nn + 8 nr (0: not conductive)
+            // factor = nn + nr * k_0 in float32, inf where 0 (:47-55, electrode.py:46-62),
+            // looked up by code in lut (fill_electrode_divisors)
             sum = __fadd_rn(comp(xp, i), comp(xm, i));
             sum = __fadd_rn(sum, comp(yp, i));
             sum = __fadd_rn(sum, comp(ym, i));
             sum = __fadd_rn(sum, comp(zp, i));
             sum = __fadd_rn(sum, comp(zm, i));
             if (RHS) sum = __fadd_rn(sum, comp(rv, i));
-            const uint32_t cd = byte_of(cc, i);
-            float div = __int_as_float(0x7f800000);
-            if (cd != 0u) {
-                const uint32_t m = cd - 1u;
-                const float d = __fadd_rn(static_cast<float>(m & 7u), __fmul_rn(static_cast<float>(m >> 3), lut[0]));
-                if (d != 0.0f) div = d;
-            }
-            quot = quotient(sum, div);
+            // lut[code]: the divisor nn + nr * k_0 of the code, inf where 0 or not conductive
+            quot = quotient(sum, lut[byte_of(cc, i)]);
         } else if (KIND == TF_KIND_ANISOTROPIC) {
             // taufactor.py:475-477: (x+1 + x-1) + Ky*(y+1 + y-1) + Kz*(z+1 + z-1)
             sum = __fadd_rn(comp(xp, i), comp(xm, i));
