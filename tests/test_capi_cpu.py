@@ -257,3 +257,21 @@ def test_label_map_and_sums_refuse_bad_arguments(lib):
     assert lib.tf_label_sums(0, 4, 4, 4, P, P, P, 3, P, None) == _capi.TF_ERR_ARG
     assert lib.tf_label_sums(1, 4, 4, 4, P, None, P, 3, P, None) == _capi.TF_ERR_ARG
     assert lib.tf_launch_count() == n0
+
+
+def test_default_kernel_configuration_per_operator_kind():
+    """Untuned solvers start from the measured best tile and fused depth of their kind: the
+    binary kind on 16 x 128 tiles when z spans a tile, multiphase 3 half-sweeps per launch,
+    the others 4 on 16 x 64 tiles."""
+    from types import SimpleNamespace
+
+    from taufactor_gb300.autotune import default_config
+
+    def fake(kind, nz):
+        return SimpleNamespace(_op=SimpleNamespace(kind=kind), Nz=nz)
+
+    assert default_config(fake(_capi.TF_KIND_BINARY, 256)) == (1, 4)
+    assert default_config(fake(_capi.TF_KIND_BINARY, 64)) == (0, 4)
+    assert default_config(fake(_capi.TF_KIND_MULTIPHASE, 320)) == (0, 3)
+    assert default_config(fake(_capi.TF_KIND_ELECTRODE, 256)) == (0, 4)
+    assert default_config(fake(_capi.TF_KIND_ANISOTROPIC, 256)) == (0, 4)
