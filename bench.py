@@ -994,6 +994,14 @@ def run_profile(args):
         torch.cuda.synchronize()
         print(f"profile workload done: electrode {args.batch}x{args.side}^3, {args.half_sweeps} half-sweeps")
         return
+    if args.anisotropic:  # AnisotropicSolver, spacing (1, 1.3, 0.7), on --batch volumes of the main workload
+        s = tg.AnisotropicSolver(batch_256(args.batch, args.side, SIGMA), (1.0, 1.3, 0.7), device="cuda")
+        s._advance(8)
+        torch.cuda.synchronize()
+        s._advance(args.half_sweeps)
+        torch.cuda.synchronize()
+        print(f"profile workload done: anisotropic {args.batch}x{args.side}^3, {args.half_sweeps} half-sweeps")
+        return
     if args.multiphase:  # MultiPhaseSolver on the three-label --side^3 volume, --half-sweeps half-sweeps
         from taufactor_gb300.synthetic import three_phase
 
@@ -1054,6 +1062,8 @@ def main():
     ap.add_argument("--multigrid", action="store_true",
                     help="--profile: one multigrid-PCG FP64 correction of a --side^3 kappa field")
     ap.add_argument("--impedance", action="store_true", help="--profile: ImpedanceSolver on one volume")
+    ap.add_argument("--anisotropic", action="store_true",
+                    help="--profile: AnisotropicSolver (spacing 1, 1.3, 0.7) on --batch volumes of the workload")
     ap.add_argument("--electrode", action="store_true",
                     help="--profile: ElectrodeSolver on --batch three-label --side^3 volumes")
     ap.add_argument("--uneven", action="store_true", help="--profile: one batched solve of the uneven batch")
